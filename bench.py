@@ -1,0 +1,319 @@
+#!/usr/bin/env python
+"""Benchmark: 30-qubit depth-20 random SU(2)/SU(4) circuit, gates/s.
+
+One step = reset a 30-qubit state to |0...0> and run the whole 900-gate
+circuit (per layer: a Haar SU(2) on every qubit, then a Haar SU(4) on each
+pair of a random perfect matching; seeded synthetic input) through the fused
+FP32 path, state resident in HBM.  The line also reports the plain FP64 path
+on the same circuit, the fused-FP32 vs FP64 fidelity and max amplitude
+error, 4096 shots sampled from both states with the same uniform draws, the
+tile kernel's roofline, an end-to-end number through the public API with
+host buffers, and a CPU baseline (the oracle restatement of the reference's
+per-gate algorithm on the host cores).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Under torchrun each rank runs an independent replica on its own GPU
+(the workload does not shard); value = all ranks' gates / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "30q gates/s fused-FP32 vs plain FP64 at fidelity>=1-1e-6; %HBM peak; p99 latency"
+UNIT = "gates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=20)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--shots", type=int, default=4096)
+    ap.add_argument("--fw", type=int, default=2)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(n, gates, seconds, threads):
+    """The oracle (restatement of the reference's per-gate apply-matrix-
+    operator with worker-parallel loops) on the host cores: a bounded sample
+    of the same circuit -- its first gates, until `seconds` have passed."""
+    from oracle import oracle as O
+    O.set_workers(threads, threshold=19)
+    wf = O.zero_state(n)
+    t0 = time.perf_counter()
+    done = 0
+    for m, qs in gates:
+        O.apply_matrix_operator(wf, m, qs)
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    del wf
+    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {done} of {len(gates)} gates of the {n}-qubit circuit, FP64, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist()
+    if rank != 0:
+        return
+    from qvm_gb300 import circuits
+    gates = circuits.random_su_circuit(args.n, args.depth, args.seed)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, min(args.cpu_seconds, 20.0))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(args.n, gates, per_step if i >= args.warmup else 1.0, threads)
+        if i >= args.warmup:
+            vals.append(r)
+    value = float(np.mean([v["value"] for v in vals]))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * len(gates) / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Haar SU(2)/SU(4) circuit)", "impl": "reference",
+            "config": {"workload": f"random SU(2)/SU(4) circuit, {args.n} qubits, depth "
+                                   f"{args.depth}, {len(gates)} gates",
+                       "cpu": "oracle restatement of the reference's apply-matrix-operator "
+                              "(no SBCL on this host)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": vals[-1]["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    ws, rank, local = dist()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from qvm_gb300 import CudaPureState, Program, circuits
+    from qvm_gb300.state import PRECISIONS  # noqa: F401
+
+    n = args.n
+    gates = circuits.random_su_circuit(n, args.depth, args.seed)
+    G = len(gates)
+    prog = Program()
+    prog.add_gates(gates)
+    stats = prog.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
+    s32 = CudaPureState(n, "fp32")
+    stream = torch.cuda.ExternalStream(s32.stream())
+
+    def step():
+        s32.set_to_zero_state()
+        return prog.run_profiled(s32, fused=True)
+
+    for _ in range(args.warmup):
+        step()
+    s32.sync()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    step_ms, tile_ms, launches = [], [], 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ms, kinds = step()
+        b.record(stream)
+        b.synchronize()
+        step_ms.append(a.elapsed_time(b))
+        tile_ms.extend(ms[kinds == 3].tolist())
+        launches += len(ms) + 1  # passes + the |0> amplitude kernel
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    total_ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * G * args.steps / (total_ms / 1e3)
+
+    result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+              "data": "synthetic (seeded Haar SU(2)/SU(4) circuit)"}
+    state_bytes = (1 << n) * 8
+    result["config"] = {
+        "workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth {args.depth}, {G} gates, "
+                    f"fused FP32 (fusion width {args.fw})",
+        "passes": stats["passes"], "fused_blocks": stats["fused_blocks"],
+        "state_bytes": state_bytes,
+        "l2": "state (%.1f GiB) is larger than L2; no flush needed" % (state_bytes / 2 ** 30),
+        "parallelism": f"replicas x{ws}"}
+    result["latency_ms"] = {"p50": float(np.percentile(step_ms, 50)),
+                            "p99": float(np.percentile(step_ms, 99)), "what": "one circuit run"}
+    peak, peak_kind = peaks()
+    if tile_ms:
+        avg = float(np.mean(tile_ms))
+        ach = 2 * state_bytes / (avg / 1e3) / 1e9
+        result["roofline"] = {"bound": "hbm", "kernel": "k_tile<float>", "achieved": ach,
+                              "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                              "peak_source": peak_kind,
+                              "algorithmic_bytes_per_launch": 2 * state_bytes,
+                              "avg_launch_ms": avg, "traffic": None}
+    result["gpu_launches"] = launches
+    result["clocks"] = clk
+
+    # --- end to end through the public API with host buffers --------------------
+    draws = np.random.default_rng(args.seed + 1).random(args.shots)
+    e2e_ms = []
+    h2d = d2h = 0
+    for i in range(max(2, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        p = Program()
+        p.add_gates(gates)               # host gate matrices
+        st = p.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
+        s32.set_to_zero_state()
+        p.run(s32, fused=True)           # plan upload + passes
+        shots = s32.sample(draws)        # draws H2D, shot indices D2H
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        h2d = st.get("upload_bytes", 0) + draws.nbytes
+        d2h = shots.nbytes
+        p.free()
+    result["e2e"] = {"value": G / (np.median(e2e_ms[1:]) / 1e3), "unit": UNIT,
+                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                     "what": "Program build + plan + upload + run + 4096 shots via the C ABI"}
+
+    # --- plain FP64 comparison, fidelity, shots --------------------------------------
+    if not args.no_fp64 and rank == 0:
+        s64 = CudaPureState(n, "fp64")
+        pp = Program()
+        pp.add_gates(gates[:8])
+        pp.run(s64, fused=False)       # warm-up on a prefix
+        s64.set_to_zero_state()
+        s64.sync()
+        st64 = torch.cuda.ExternalStream(s64.stream())
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st64)
+        prog.run(s64, fused=False)
+        b.record(st64)
+        b.synchronize()
+        ms64 = a.elapsed_time(b)
+        s32.set_to_zero_state()
+        prog.run(s32, fused=True)
+        f, err = s64.fidelity(s32)
+        sh64 = s64.sample(draws)
+        sh32 = s32.sample(draws)
+        result["plain_fp64"] = {"gates_per_s": G / (ms64 / 1e3), "ms": ms64,
+                                "speedup_fused_fp32": (G / (ms64 / 1e3)) and value / ws /
+                                (G / (ms64 / 1e3))}
+        result["fidelity"] = {"fused_fp32_vs_fp64": f, "max_abs_err": err,
+                              "shots": int(args.shots),
+                              "identical_shots": int((sh64 == sh32).sum())}
+        s64.free()
+    if not args.no_cpu and rank == 0:
+        result["cpu_baseline"] = cpu_baseline(n, gates, args.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    s32.free()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,195 @@
+/*
+ * qvmgpu.h -- C ABI of the GB300 (sm_103a) statevector engine for the QVM.
+ *
+ * This library is the drop-in replacement for the Lisp pure-state
+ * representation of quil-lang/qvm.  A Lisp host (SBCL + CFFI) or any other
+ * C-ABI caller owns opaque state handles whose amplitudes live in GPU HBM.
+ * Every entry point below names the reference interface it replaces
+ * (file:line in the quil-lang/qvm source tree).
+ *
+ * Conventions
+ *  - Amplitude layout: index bit q = qubit q (LSB first).  Host buffers are
+ *    complex128 (interleaved re, im doubles; 16 bytes per amplitude), the
+ *    layout of the reference's (simple-array (complex double-float))
+ *    (src/floats.lisp:13-27, scripts/shared_qvm.py:34-42).
+ *  - Qubit tuples are nat-tuples (src/utilities.lisp:43-51): qubits[0] is
+ *    bit 0 of the gate matrix's row/column index, i.e. the LAST argument of
+ *    the Quil gate application "G a b" -> qubits = {b, a}.
+ *  - Matrices are row-major 2^k x 2^k complex128.
+ *  - Every function returns 0 (QVMG_OK) or a qvmg_status code; the message
+ *    of the last failure on the calling thread is qvmg_last_error().
+ *  - Random draws are supplied by the caller (the host keeps its MT19937
+ *    stream and the reference's draw order), so results are reproducible.
+ *  - Calls on one state are ordered on that state's own CUDA stream; calls
+ *    on distinct states may run concurrently from different threads.
+ */
+#ifndef QVMGPU_H
+#define QVMGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QVMG_ABI_VERSION 1
+#define QVMG_MAX_QUBITS 34       /* 2^34 FP64 amplitudes = 256 GiB */
+#define QVMG_MAX_GATE_QUBITS 5   /* per-op width of the dense/permutation ABI */
+#define QVMG_MAX_DIAG_QUBITS 10  /* per-op width of the diagonal ABI */
+
+typedef enum {
+  QVMG_FP64 = 0, /* complex double: the reference's cflonum */
+  QVMG_FP32 = 1  /* complex float: the fused split-precision form */
+} qvmg_precision;
+
+typedef enum {
+  QVMG_OK = 0,
+  QVMG_E_INVALID = 1,     /* bad argument (qubit out of range, bad k, ...) */
+  QVMG_E_CUDA = 2,        /* a CUDA runtime call failed */
+  QVMG_E_NOMEM = 3,       /* device allocation failed */
+  QVMG_E_RANGE = 4,       /* probability out of range for a forced outcome */
+  QVMG_E_UNSUPPORTED = 5, /* valid request this build does not handle */
+  QVMG_E_TIMEOUT = 6      /* a bounded device-side wait gave up */
+} qvmg_status;
+
+typedef enum {
+  /* src/measurement.lisp:87-105: p1 = P(q=1); no draw is consumed when
+   * p1 = 0; otherwise bit = 1 iff draw <= p1. */
+  QVMG_MEASURE_INTERPRETED = 0,
+  /* src/compile-gate.lisp:221-254: p0 = P(q=0); the draw is always
+   * consumed; bit = 0 iff draw < p0. */
+  QVMG_MEASURE_COMPILED = 1
+} qvmg_measure_convention;
+
+typedef enum {
+  /* src/measurement.lisp:179-225: smallest b with C(b) > p (len-1 if none). */
+  QVMG_SAMPLE_BISECT = 0,
+  /* src/measurement.lisp:246-288: smallest i with C(i) >= p (len-1 if none). */
+  QVMG_SAMPLE_CDF = 1
+} qvmg_sample_rule;
+
+typedef enum {
+  QVMG_RUN_PLAIN = 0, /* one pass per source gate, like apply-matrix-operator */
+  QVMG_RUN_FUSED = 1  /* gate fusion + shared-memory tile passes */
+} qvmg_run_mode;
+
+typedef struct qvmg_state_s *qvmg_state;
+typedef struct qvmg_program_s *qvmg_program;
+
+/* ---- library ------------------------------------------------------------ */
+const char *qvmg_last_error(void);
+int qvmg_abi_version(void);
+/* Device facts for admission control: SM count, free/total HBM bytes. */
+int qvmg_device_info(int *sm_count, uint64_t *free_bytes, uint64_t *total_bytes);
+/* HBM bytes a state of this size and precision holds (16*2^n or 8*2^n plus
+ * its reduction scratch); 0 for invalid arguments. */
+uint64_t qvmg_state_bytes(int nqubits, int precision);
+
+/* ---- state protocol (src/state-representation.lisp) ----------------------- */
+/* make-pure-state :76-101 + allocate-vector (src/allocator.lisp:47-62):
+ * allocate 2^n amplitudes in HBM set to |0...0>. */
+int qvmg_state_create(int nqubits, int precision, qvmg_state *out);
+/* The finalizer returned by allocate-vector (src/allocator.lisp:33-62). */
+int qvmg_state_free(qvmg_state s);
+/* num-qubits :138-140 */
+int qvmg_state_info(qvmg_state s, int *nqubits, int *precision);
+/* set-to-zero-state :150-152 -> bring-to-zero-state (src/wavefunction.lisp:80-91) */
+int qvmg_state_reset(qvmg_state s);
+/* (setf state-elements) :130-132: load 2^n complex128 amplitudes. */
+int qvmg_state_upload(qvmg_state s, const double *amps);
+/* state-elements :134-136 / amplitudes: read 2^n complex128 amplitudes. */
+int qvmg_state_download(qvmg_state s, double *amps);
+/* copy-wavefunction (src/wavefunction.lisp:93-109); both states must have
+ * the same qubit count; precisions may differ (converted on the device). */
+int qvmg_state_copy(qvmg_state dst, qvmg_state src);
+/* Wait for all work queued on the state. */
+int qvmg_state_sync(qvmg_state s);
+
+/* ---- gate application (src/apply-gate.lisp:106-181) ---------------------- */
+/* apply-matrix-operator (src/wavefunction.lisp:308-330) with the serial
+ * kernels (src/serial-kernels.lisp:19-288): dense k-qubit matrix, k <= 5.
+ * Diagonal and permutation matrices are routed to the kernels below, the
+ * way compile-gate specialises constant matrices (src/compile-gate.lisp). */
+int qvmg_apply_dense(qvmg_state s, int k, const int *qubits, const double *matrix);
+/* Permutation gate (src/compile-gate.lisp:259-309): within each group,
+ * new amplitude j = old amplitude perm[j]; k <= 5. */
+int qvmg_apply_permutation(qvmg_state s, int k, const int *qubits, const int64_t *perm);
+/* Diagonal gate (RZ, CPHASE, CZ, RZZ, PHASE, S, T ...): amplitude with
+ * sub-index j is multiplied by diag[j] (2^k complex128); k <= 10. */
+int qvmg_apply_diagonal(qvmg_state s, int k, const int *qubits, const double *diag);
+
+/* ---- measurement (src/measurement.lisp) ----------------------------------- */
+/* wavefunction-excited-state-probability (src/wavefunction.lisp:62-70),
+ * get-excited-state-probability (src/measurement.lisp:71-75); FP64 sum. */
+int qvmg_prob_excited(qvmg_state s, int q, double *p1);
+/* wavefunction-ground-state-probability (src/wavefunction.lisp:52-60) */
+int qvmg_prob_ground(qvmg_state s, int q, double *p0);
+/* force-measurement (src/measurement.lisp:10-41): zero the amplitudes with
+ * bit q != bit and scale the rest by 1/sqrt(P(bit)), one pass. */
+int qvmg_force_measurement(qvmg_state s, int q, int bit, double excited_probability);
+/* measure (src/measurement.lisp:87-105) or the compiled measurement
+ * (src/compile-gate.lisp:221-254): probability, draw, collapse.  *prob is
+ * p1 (interpreted) or p0 (compiled); *draw_used is 0 when no draw was
+ * consumed.  Any output pointer may be NULL. */
+int qvmg_measure(qvmg_state s, int q, double draw, int convention, int *bit,
+                 int *draw_used, double *prob);
+/* measure-all-state (src/measurement.lisp:128-143): sample by the bisection
+ * rule with one draw, then collapse to the basis state e_b (amplitude 1). */
+int qvmg_measure_all(qvmg_state s, double draw, uint64_t *index);
+/* Multishot sampling without collapse: one basis index per draw, by the
+ * bisection rule (what repeated measure-all on a reloaded copy returns,
+ * app/src/api/multishot-measure.lisp:93-109) or the CDF rule
+ * (sample-wavefunction-multiple-times, src/measurement.lisp:246-288). */
+int qvmg_sample(qvmg_state s, const double *draws, uint64_t nshots, int rule,
+                uint64_t *out);
+/* |a_i|^2 for every amplitude (app/src/api/probabilities.lisp:13-19). */
+int qvmg_probabilities(qvmg_state s, double *out);
+/* norm / normalize-wavefunction (src/wavefunction.lisp:332-364). */
+int qvmg_norm(qvmg_state s, double *norm);
+int qvmg_normalize(qvmg_state s);
+/* inner product sum conj(a_i) b_i (app/src/api/expectation.lisp:80-84). */
+int qvmg_inner(qvmg_state a, qvmg_state b, double *re, double *im);
+/* |<a|b>|^2 and max_i |a_i - b_i| (precision report of the fused form). */
+int qvmg_fidelity(qvmg_state a, qvmg_state b, double *fidelity, double *max_abs_err);
+
+/* ---- programs: transition loop over gate applications ------------------- */
+/* A program is the gate-application part of a loaded Quil program
+ * (src/classical-memory-mixin.lisp:114-159, src/execution.lisp:31-37), as a
+ * list of ops.  QVMG_RUN_PLAIN applies them one pass per op (the
+ * reference's transition -> apply-gate-to-state loop); QVMG_RUN_FUSED runs
+ * them through the gate-fusion pass (the compile-loaded-program hook,
+ * src/qvm.lisp:166-175) and shared-memory tile passes. */
+int qvmg_program_create(qvmg_program *out);
+int qvmg_program_free(qvmg_program p);
+int qvmg_program_add_dense(qvmg_program p, int k, const int *qubits, const double *matrix);
+int qvmg_program_add_permutation(qvmg_program p, int k, const int *qubits, const int64_t *perm);
+int qvmg_program_add_diagonal(qvmg_program p, int k, const int *qubits, const double *diag);
+int qvmg_program_num_ops(qvmg_program p, int *nops);
+/* Plan (host only, no GPU work): fusion width (max qubits of a fused block,
+ * 1..QVMG_MAX_GATE_QUBITS) and tile width (qubits held per shared-memory
+ * tile, 0 = default).  *npasses receives the number of device passes. */
+int qvmg_program_plan(qvmg_program p, int nqubits, int precision, int mode,
+                      int fusion_width, int tile_qubits, int *npasses);
+/* Plan statistics: stats[0]=source ops, [1]=passes, [2]=tile passes,
+ * [3]=fused blocks, [4]=diagonal passes, [5]=permutation passes,
+ * [6]=algorithmic bytes moved per run (2 x state bytes x passes),
+ * [7]=bytes of op data and descriptors a run uploads to the device. */
+int qvmg_program_plan_stats(qvmg_program p, int64_t *stats, int nstats);
+/* JSON text of the last plan (passes, tile qubits, op data) for tools and
+ * tests; *needed receives the buffer size required (with the NUL). */
+int qvmg_program_plan_describe(qvmg_program p, char *buf, uint64_t cap, uint64_t *needed);
+/* Run the program on the state (plans on first use for the state's size). */
+int qvmg_program_run(qvmg_state s, qvmg_program p, int mode);
+/* Same, recording a CUDA event around every pass on the state's stream;
+ * waits for the run and writes each pass's device time (ms) and kind
+ * (0 dense, 1 diagonal, 2 permutation, 3 tile) for up to `cap` passes. */
+int qvmg_program_run_profiled(qvmg_state s, qvmg_program p, int mode, float *pass_ms,
+                              int *pass_kind, int cap, int *npasses);
+/* The cudaStream_t (as void*) the state's work is ordered on, so a caller
+ * can order or time its own work against it. */
+int qvmg_state_stream(qvmg_state s, void **stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

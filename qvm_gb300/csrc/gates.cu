@@ -1,0 +1,388 @@
+// gates.cu -- per-gate ("plain") kernels: one HBM pass per source gate.
+//
+// These replace the reference's apply-matrix-operator and its serial /
+// AVX2 kernels (src/wavefunction.lisp:271-330, src/serial-kernels.lisp:
+// 19-288, src/impl/sbcl-avx-vops.lisp) and the compiled permutation gates
+// (src/compile-gate.lisp:259-309):
+//  - k_dense<K>: for each of the 2^(n-K) groups (complement indices with K
+//    zero bits injected, src/wavefunction.lisp:155-175), gather the 2^K
+//    amplitudes into registers, multiply by the matrix held in the kernel's
+//    parameter bank (uniform across the warp), scatter back.  128-bit loads
+//    (one double2 / float2 per amplitude), grid-stride over groups.
+//  - k_perm<K>: only the amplitudes a permutation moves are read/written.
+//  - k_diag_tables: a run of diagonal gates is folded on the host into at
+//    most kMaxTables phase tables over <= 10 qubits each; each amplitude's
+//    phase is the product of its table entries; amplitudes whose phase is
+//    exactly 1 are neither read nor written.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cplx.h"
+#include "internal.h"
+
+namespace qvmg {
+
+template <typename T, int K>
+struct DenseArgs {
+  typename CT<T>::C m[(1 << K) * (1 << K)];  // row-major
+  uint64_t off[1 << K];                      // address offset of sub-index c
+  int sorted[K];                             // gate qubits, ascending
+};
+
+template <typename T, int K, bool REAL>
+__global__ void __launch_bounds__(256)
+    k_dense(typename CT<T>::C *__restrict__ a, uint64_t ngroups,
+            const __grid_constant__ DenseArgs<T, K> p) {
+  using C = typename CT<T>::C;
+  constexpr int D = 1 << K;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < ngroups;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t base = g;
+#pragma unroll
+    for (int s = 0; s < K; ++s) base = inject0(base, p.sorted[s]);
+    C v[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = a[base + p.off[c]];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      C acc = CT<T>::make(0, 0);
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        if (REAL)
+          rmac(acc, p.m[r * D + c].x, v[c]);
+        else
+          cmac(acc, p.m[r * D + c], v[c]);
+      }
+      a[base + p.off[r]] = acc;
+    }
+  }
+}
+
+template <int K>
+struct PermArgs {
+  uint64_t off[1 << K];
+  int sorted[K];
+  int nmoved;
+  unsigned char dst[1 << K];
+  unsigned char src[1 << K];
+};
+
+template <typename T, int K>
+__global__ void __launch_bounds__(256)
+    k_perm(typename CT<T>::C *__restrict__ a, uint64_t ngroups,
+           const __grid_constant__ PermArgs<K> p) {
+  using C = typename CT<T>::C;
+  constexpr int D = 1 << K;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < ngroups;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t base = g;
+#pragma unroll
+    for (int s = 0; s < K; ++s) base = inject0(base, p.sorted[s]);
+    C v[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j)
+      if (j < p.nmoved) v[j] = a[base + p.off[p.src[j]]];
+#pragma unroll
+    for (int j = 0; j < D; ++j)
+      if (j < p.nmoved) a[base + p.off[p.dst[j]]] = v[j];
+  }
+}
+
+constexpr int kMaxTables = 4;
+constexpr int kMaxTableBits = 10;
+
+struct DiagArgs {
+  int ntables;
+  int k[kMaxTables];
+  int qubits[kMaxTables][kMaxTableBits];
+  int start[kMaxTables];  // entry offset of each table
+  int total;              // total entries
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_diag_tables(typename CT<T>::C *__restrict__ a, uint64_t len,
+                  const typename CT<T>::C *__restrict__ tables,
+                  const __grid_constant__ DiagArgs p) {
+  using C = typename CT<T>::C;
+  extern __shared__ unsigned char smem_raw[];
+  C *tab = reinterpret_cast<C *>(smem_raw);
+  for (int j = threadIdx.x; j < p.total; j += blockDim.x) tab[j] = tables[j];
+  __syncthreads();
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    C ph = CT<T>::make(1, 0);
+    for (int t = 0; t < p.ntables; ++t) {
+      int idx = 0;
+      for (int j = 0; j < p.k[t]; ++j) idx |= (int)((i >> p.qubits[t][j]) & 1ull) << j;
+      C e = tab[p.start[t] + idx];
+      ph = (t == 0) ? e : cmul(ph, e);
+    }
+    if (ph.x != (T)1 || ph.y != (T)0) a[i] = cmul(a[i], ph);
+  }
+}
+
+// ---- host side ------------------------------------------------------------------
+
+static void sorted_qubits(int k, const int *qubits, int *sorted) {
+  std::copy(qubits, qubits + k, sorted);
+  std::sort(sorted, sorted + k);
+}
+
+template <typename T, int K>
+static int dense_impl(qvmg_state s, const int *qubits, const double *m, bool real) {
+  using C = typename CT<T>::C;
+  constexpr int D = 1 << K;
+  DenseArgs<T, K> p;
+  for (int i = 0; i < D * D; ++i) p.m[i] = CT<T>::make((T)m[2 * i], (T)m[2 * i + 1]);
+  for (int c = 0; c < D; ++c) {
+    uint64_t o = 0;
+    for (int j = 0; j < K; ++j)
+      if ((c >> j) & 1) o |= 1ull << qubits[j];
+    p.off[c] = o;
+  }
+  sorted_qubits(K, qubits, p.sorted);
+  uint64_t ngroups = s->len >> K;
+  int grid = grid_for(ngroups, 256);
+  C *a = (C *)s->amps;
+  if (real)
+    k_dense<T, K, true><<<grid, 256, 0, s->stream>>>(a, ngroups, p);
+  else
+    k_dense<T, K, false><<<grid, 256, 0, s->stream>>>(a, ngroups, p);
+  QVMG_CHECK_LAUNCH("k_dense");
+  return QVMG_OK;
+}
+
+template <typename T>
+static int dense_dispatch(qvmg_state s, int k, const int *qubits, const double *m, bool real) {
+  switch (k) {
+    case 1: return dense_impl<T, 1>(s, qubits, m, real);
+    case 2: return dense_impl<T, 2>(s, qubits, m, real);
+    case 3: return dense_impl<T, 3>(s, qubits, m, real);
+    case 4: return dense_impl<T, 4>(s, qubits, m, real);
+    case 5: return dense_impl<T, 5>(s, qubits, m, real);
+  }
+  return fail(QVMG_E_INVALID, "dense gate width must be 1..5");
+}
+
+template <typename T, int K>
+static int perm_impl(qvmg_state s, const int *qubits, const int64_t *perm) {
+  using C = typename CT<T>::C;
+  constexpr int D = 1 << K;
+  PermArgs<K> p;
+  for (int c = 0; c < D; ++c) {
+    uint64_t o = 0;
+    for (int j = 0; j < K; ++j)
+      if ((c >> j) & 1) o |= 1ull << qubits[j];
+    p.off[c] = o;
+  }
+  sorted_qubits(K, qubits, p.sorted);
+  p.nmoved = 0;
+  for (int j = 0; j < D; ++j) {
+    if (perm[j] != j) {
+      p.dst[p.nmoved] = (unsigned char)j;
+      p.src[p.nmoved] = (unsigned char)perm[j];
+      ++p.nmoved;
+    }
+  }
+  if (p.nmoved == 0) return QVMG_OK;
+  uint64_t ngroups = s->len >> K;
+  k_perm<T, K><<<grid_for(ngroups, 256), 256, 0, s->stream>>>((C *)s->amps, ngroups, p);
+  QVMG_CHECK_LAUNCH("k_perm");
+  return QVMG_OK;
+}
+
+template <typename T>
+static int perm_dispatch(qvmg_state s, int k, const int *qubits, const int64_t *perm) {
+  switch (k) {
+    case 1: return perm_impl<T, 1>(s, qubits, perm);
+    case 2: return perm_impl<T, 2>(s, qubits, perm);
+    case 3: return perm_impl<T, 3>(s, qubits, perm);
+    case 4: return perm_impl<T, 4>(s, qubits, perm);
+    case 5: return perm_impl<T, 5>(s, qubits, perm);
+  }
+  return fail(QVMG_E_INVALID, "permutation width must be 1..5");
+}
+
+static int diag_args(int ntables, const int *ks, const int *qubits, DiagArgs &p) {
+  std::memset(&p, 0, sizeof(p));
+  p.ntables = ntables;
+  int total = 0, qoff = 0;
+  for (int t = 0; t < ntables; ++t) {
+    p.k[t] = ks[t];
+    for (int j = 0; j < ks[t]; ++j) p.qubits[t][j] = qubits[qoff + j];
+    qoff += ks[t];
+    p.start[t] = total;
+    total += 1 << ks[t];
+  }
+  p.total = total;
+  return total;
+}
+
+template <typename T>
+static int diag_dev_impl(qvmg_state s, const DiagArgs &p, const void *dtables) {
+  using C = typename CT<T>::C;
+  size_t smem = p.total * sizeof(C);
+  k_diag_tables<T><<<grid_for(s->len, 256), 256, smem, s->stream>>>(
+      (C *)s->amps, s->len, (const C *)dtables, p);
+  QVMG_CHECK_LAUNCH("k_diag_tables");
+  return QVMG_OK;
+}
+
+template <typename T>
+static int diag_tables_impl(qvmg_state s, int ntables, const int *ks, const int *qubits,
+                            const double *tables) {
+  using C = typename CT<T>::C;
+  DiagArgs p;
+  int total = diag_args(ntables, ks, qubits, p);
+  std::vector<C> host(total);
+  for (int i = 0; i < total; ++i) host[i] = CT<T>::make((T)tables[2 * i], (T)tables[2 * i + 1]);
+  int rc = ensure_dvec(s, total * sizeof(C));
+  if (rc) return rc;
+  QVMG_CUDA(cudaMemcpyAsync(s->dvec, host.data(), total * sizeof(C), cudaMemcpyHostToDevice,
+                            s->stream));
+  // The host vector dies at return: make sure the copy has consumed it.
+  QVMG_CUDA(cudaStreamSynchronize(s->stream));
+  return diag_dev_impl<T>(s, p, s->dvec);
+}
+
+// Attribute setup for the large-smem diagonal kernel.
+static bool g_diag_attr_done = false;
+static int diag_attr() {
+  if (g_diag_attr_done) return QVMG_OK;
+  int bytes = kMaxTables * (1 << kMaxTableBits) * 16;
+  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables<double>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables<float>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  g_diag_attr_done = true;
+  return QVMG_OK;
+}
+
+int launch_diag_tables(qvmg_state s, int ntables, const int *ks, const int *qubits,
+                       const double *tables) {
+  if (ntables < 1 || ntables > kMaxTables)
+    return fail(QVMG_E_INVALID, "diagonal pass needs 1..4 tables");
+  for (int t = 0; t < ntables; ++t)
+    if (ks[t] < 1 || ks[t] > kMaxTableBits)
+      return fail(QVMG_E_INVALID, "diagonal table width must be 1..10");
+  int rc = diag_attr();
+  if (rc) return rc;
+  if (s->prec == QVMG_FP64) return diag_tables_impl<double>(s, ntables, ks, qubits, tables);
+  return diag_tables_impl<float>(s, ntables, ks, qubits, tables);
+}
+
+int launch_diag_dev(qvmg_state s, int ntables, const int *ks, const int *qubits,
+                    const void *dtables) {
+  if (ntables < 1 || ntables > kMaxTables)
+    return fail(QVMG_E_INVALID, "diagonal pass needs 1..4 tables");
+  int rc = diag_attr();
+  if (rc) return rc;
+  DiagArgs p;
+  diag_args(ntables, ks, qubits, p);
+  if (s->prec == QVMG_FP64) return diag_dev_impl<double>(s, p, dtables);
+  return diag_dev_impl<float>(s, p, dtables);
+}
+
+int launch_dense(qvmg_state s, int k, const int *qubits, const double *m) {
+  bool real = true;
+  for (int i = 0; i < (1 << (2 * k)); ++i)
+    if (m[2 * i + 1] != 0.0) { real = false; break; }
+  if (s->prec == QVMG_FP64) return dense_dispatch<double>(s, k, qubits, m, real);
+  return dense_dispatch<float>(s, k, qubits, m, real);
+}
+
+int launch_permutation(qvmg_state s, int k, const int *qubits, const int64_t *perm) {
+  if (s->prec == QVMG_FP64) return perm_dispatch<double>(s, k, qubits, perm);
+  return perm_dispatch<float>(s, k, qubits, perm);
+}
+
+int launch_diagonal(qvmg_state s, int k, const int *qubits, const double *diag) {
+  return launch_diag_tables(s, 1, &k, qubits, diag);
+}
+
+// Matrix classification: the compile-gate specialisations of constant
+// matrices (src/compile-gate.lisp:113-209, :259-309).
+bool matrix_is_diagonal(int k, const double *m) {
+  int d = 1 << k;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c)
+      if (r != c && (m[2 * (r * d + c)] != 0.0 || m[2 * (r * d + c) + 1] != 0.0)) return false;
+  return true;
+}
+
+bool matrix_is_permutation(int k, const double *m, int64_t *perm) {
+  int d = 1 << k;
+  std::vector<int> seen(d, 0);
+  for (int r = 0; r < d; ++r) {
+    int one = -1;
+    for (int c = 0; c < d; ++c) {
+      double re = m[2 * (r * d + c)], im = m[2 * (r * d + c) + 1];
+      if (re == 1.0 && im == 0.0) {
+        if (one >= 0) return false;
+        one = c;
+      } else if (re != 0.0 || im != 0.0) {
+        return false;
+      }
+    }
+    if (one < 0 || seen[one]) return false;
+    seen[one] = 1;
+    perm[r] = one;
+  }
+  return true;
+}
+
+}  // namespace qvmg
+
+using namespace qvmg;
+
+extern "C" {
+
+int qvmg_apply_dense(qvmg_state s, int k, const int *qubits, const double *matrix) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if ((rc = check_qubits(s, k, qubits, QVMG_MAX_GATE_QUBITS))) return rc;
+  if (!matrix) return fail(QVMG_E_INVALID, "null matrix");
+  int64_t perm[32];
+  if (matrix_is_permutation(k, matrix, perm)) return launch_permutation(s, k, qubits, perm);
+  if (matrix_is_diagonal(k, matrix)) {
+    std::vector<double> diag(2 << k);
+    int d = 1 << k;
+    for (int j = 0; j < d; ++j) {
+      diag[2 * j] = matrix[2 * (j * d + j)];
+      diag[2 * j + 1] = matrix[2 * (j * d + j) + 1];
+    }
+    return launch_diagonal(s, k, qubits, diag.data());
+  }
+  return launch_dense(s, k, qubits, matrix);
+}
+
+int qvmg_apply_permutation(qvmg_state s, int k, const int *qubits, const int64_t *perm) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if ((rc = check_qubits(s, k, qubits, QVMG_MAX_GATE_QUBITS))) return rc;
+  if (!perm) return fail(QVMG_E_INVALID, "null permutation");
+  int d = 1 << k;
+  std::vector<int> seen(d, 0);
+  for (int j = 0; j < d; ++j) {
+    if (perm[j] < 0 || perm[j] >= d || seen[perm[j]])
+      return fail(QVMG_E_INVALID, "not a permutation of 0..2^k-1");
+    seen[perm[j]] = 1;
+  }
+  return launch_permutation(s, k, qubits, perm);
+}
+
+int qvmg_apply_diagonal(qvmg_state s, int k, const int *qubits, const double *diag) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if ((rc = check_qubits(s, k, qubits, QVMG_MAX_DIAG_QUBITS))) return rc;
+  if (!diag) return fail(QVMG_E_INVALID, "null diagonal");
+  return launch_diagonal(s, k, qubits, diag);
+}
+
+}  // extern "C"

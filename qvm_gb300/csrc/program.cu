@@ -1,0 +1,491 @@
+// program.cu -- programs: the gate-application part of a loaded Quil program,
+// planned (plan.cpp) and run pass by pass on a state's stream.
+//
+// QVMG_RUN_PLAIN reproduces the reference's transition loop: one device
+// pass per source gate (src/execution.lisp:31-37 -> src/transition.lisp:
+// 155-186 -> apply-gate-to-state), with diagonal runs folded into phase
+// passes and permutation matrices moved as index remaps.  QVMG_RUN_FUSED
+// runs the fused + tiled plan.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "internal.h"
+#include "plan.h"
+#include "tile.h"
+
+namespace qvmg {
+
+// Device image of one plan for one precision.
+struct DevicePlan {
+  Plan plan;
+  void *buf = nullptr;                  // op descriptors + data
+  std::vector<size_t> pass_off;         // per pass: byte offset of its data
+  std::vector<TileArgs> tile_args;      // per pass (TILE passes)
+  std::vector<std::vector<int>> dks;    // per pass (DIAG passes): table widths
+  std::vector<std::vector<int>> dqs;    // per pass (DIAG passes): flat qubits
+  ~DevicePlan() {
+    if (buf) cudaFree(buf);
+  }
+};
+
+}  // namespace qvmg
+
+struct qvmg_program_s {
+  std::vector<qvmg::Op> ops;
+  std::mutex mu;
+  // key: (nq, prec, mode, fw, tile)
+  std::map<std::tuple<int, int, int, int, int>, std::unique_ptr<qvmg::DevicePlan>> plans;
+  qvmg::Plan last_plan;  // most recent host-only plan (for statistics)
+  int default_fw = 2;
+  int default_tile = 0;
+};
+
+namespace qvmg {
+
+template <typename T>
+static void put_complex(std::vector<unsigned char> &bytes, const std::vector<cd> &v) {
+  size_t off = bytes.size();
+  bytes.resize(off + v.size() * 2 * sizeof(T));
+  T *p = reinterpret_cast<T *>(bytes.data() + off);
+  for (size_t i = 0; i < v.size(); ++i) {
+    p[2 * i] = (T)v[i].real();
+    p[2 * i + 1] = (T)v[i].imag();
+  }
+}
+
+static void align16(std::vector<unsigned char> &bytes) {
+  while (bytes.size() % 16) bytes.push_back(0);
+}
+
+static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw, int tile,
+                             DevicePlan &dp) {
+  make_plan(p->ops, nq, prec, mode, fw, tile, dp.plan);
+  std::vector<unsigned char> bytes;
+  const size_t csz = prec == QVMG_FP64 ? 16 : 8;
+  dp.pass_off.assign(dp.plan.passes.size(), 0);
+  dp.tile_args.assign(dp.plan.passes.size(), TileArgs{});
+  dp.dks.assign(dp.plan.passes.size(), {});
+  dp.dqs.assign(dp.plan.passes.size(), {});
+  for (size_t i = 0; i < dp.plan.passes.size(); ++i) {
+    const Pass &ps = dp.plan.passes[i];
+    align16(bytes);
+    dp.pass_off[i] = bytes.size();
+    if (ps.kind == Pass::DIAG) {
+      for (size_t t = 0; t < ps.tq.size(); ++t) {
+        dp.dks[i].push_back((int)ps.tq[t].size());
+        for (int q : ps.tq[t]) dp.dqs[i].push_back(q);
+        if (prec == QVMG_FP64) put_complex<double>(bytes, ps.tables[t]);
+        else put_complex<float>(bytes, ps.tables[t]);
+      }
+    } else if (ps.kind == Pass::TILE) {
+      TileArgs &ta = dp.tile_args[i];
+      std::memset(&ta, 0, sizeof(ta));
+      ta.t = ps.t;
+      ta.L = ps.L;
+      ta.nE = (int)ps.E.size();
+      if (ta.nE > kTileMaxE) return fail(QVMG_E_UNSUPPORTED, "tile has too many qubits");
+      for (int e = 0; e < ta.nE; ++e) ta.E[e] = ps.E[e];
+      ta.nops = (int)ps.tops.size();
+      ta.ntiles = 1ull << (nq - ps.t);
+      // data first, then op descriptors
+      std::vector<TileOpDev> descs(ps.tops.size());
+      int ndata = 0;
+      std::vector<cd> data;
+      for (size_t o = 0; o < ps.tops.size(); ++o) {
+        const TileOpHost &th = ps.tops[o];
+        TileOpDev &d = descs[o];
+        std::memset(&d, 0, sizeof(d));
+        d.kind = th.kind;
+        d.k = (int)th.pos.size();
+        for (int j = 0; j < d.k; ++j) d.pos[j] = th.pos[j];
+        d.data = ndata;
+        if (th.kind != OP_DIAG) ta.kmax = std::max(ta.kmax, d.k);
+        if (th.kind == OP_PERM) {
+          int nm = 0;
+          for (size_t j = 0; j < th.perm.size(); ++j)
+            if (th.perm[j] != (int64_t)j) {
+              d.dst[nm] = (unsigned char)j;
+              d.src[nm] = (unsigned char)th.perm[j];
+              ++nm;
+            }
+          d.nmoved = nm;
+        } else {
+          data.insert(data.end(), th.data.begin(), th.data.end());
+          ndata += (int)th.data.size();
+        }
+      }
+      ta.ndata = ndata;
+      if (ta.kmax == 0) ta.kmax = 1;  // diagonal-only tile
+      size_t data_off = bytes.size();
+      if (prec == QVMG_FP64) put_complex<double>(bytes, data);
+      else put_complex<float>(bytes, data);
+      align16(bytes);
+      size_t ops_off = bytes.size();
+      bytes.resize(ops_off + descs.size() * sizeof(TileOpDev));
+      std::memcpy(bytes.data() + ops_off, descs.data(), descs.size() * sizeof(TileOpDev));
+      // pointers are patched after upload
+      ta.data = (const void *)data_off;
+      ta.ops = (const void *)ops_off;
+      if (tile_smem_bytes(prec, ta.t, ta.L, ta.ndata, ta.nops) > (size_t)kTileMaxSmem)
+        return fail(QVMG_E_UNSUPPORTED, "tile pass data exceeds shared memory");
+    }
+  }
+  (void)csz;
+  if (!bytes.empty()) {
+    QVMG_CUDA(cudaMalloc(&dp.buf, bytes.size()));
+    QVMG_CUDA(cudaMemcpy(dp.buf, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
+  }
+  for (size_t i = 0; i < dp.plan.passes.size(); ++i) {
+    if (dp.plan.passes[i].kind != Pass::TILE) continue;
+    TileArgs &ta = dp.tile_args[i];
+    ta.data = (const unsigned char *)dp.buf + (size_t)ta.data;
+    ta.ops = (const unsigned char *)dp.buf + (size_t)ta.ops;
+  }
+  return QVMG_OK;
+}
+
+static int run_device_plan(qvmg_state s, DevicePlan &dp, cudaEvent_t *events = nullptr) {
+  int rc = QVMG_OK;
+  if (events) QVMG_CUDA(cudaEventRecord(events[0], s->stream));
+  for (size_t i = 0; i < dp.plan.passes.size() && rc == QVMG_OK; ++i) {
+    if (events && i > 0) QVMG_CUDA(cudaEventRecord(events[i], s->stream));
+    const Pass &ps = dp.plan.passes[i];
+    switch (ps.kind) {
+      case Pass::DENSE: {
+        std::vector<double> m(2 * ps.op.m.size());
+        for (size_t j = 0; j < ps.op.m.size(); ++j) {
+          m[2 * j] = ps.op.m[j].real();
+          m[2 * j + 1] = ps.op.m[j].imag();
+        }
+        rc = launch_dense(s, ps.op.k(), ps.op.q.data(), m.data());
+        break;
+      }
+      case Pass::PERM:
+        rc = launch_permutation(s, ps.op.k(), ps.op.q.data(), ps.op.perm.data());
+        break;
+      case Pass::DIAG:
+        rc = launch_diag_dev(s, (int)dp.dks[i].size(), dp.dks[i].data(), dp.dqs[i].data(),
+                             (const unsigned char *)dp.buf + dp.pass_off[i]);
+        break;
+      case Pass::TILE:
+        rc = launch_tile(s, dp.tile_args[i]);
+        break;
+    }
+  }
+  if (events && rc == QVMG_OK)
+    QVMG_CUDA(cudaEventRecord(events[dp.plan.passes.size()], s->stream));
+  return rc;
+}
+
+static int check_op_qubits(int k, const int *qubits, int kmax) {
+  if (k < 1 || k > kmax)
+    return fail(QVMG_E_INVALID, "op width k=" + std::to_string(k) + " outside 1.." +
+                                    std::to_string(kmax));
+  if (!qubits) return fail(QVMG_E_INVALID, "null qubit tuple");
+  for (int i = 0; i < k; ++i) {
+    if (qubits[i] < 0 || qubits[i] >= QVMG_MAX_QUBITS)
+      return fail(QVMG_E_INVALID, "qubit index " + std::to_string(qubits[i]) + " out of range");
+    for (int j = 0; j < i; ++j)
+      if (qubits[i] == qubits[j])
+        return fail(QVMG_E_INVALID, "repeated qubit " + std::to_string(qubits[i]));
+  }
+  return QVMG_OK;
+}
+
+// JSON description of a plan: the passes, their qubits and op data.
+static std::string describe_plan(const Plan &pl) {
+  std::string s;
+  char tmp[96];
+  auto num = [&](double x) {
+    snprintf(tmp, sizeof(tmp), "%.17g", x);
+    s += tmp;
+  };
+  auto ints = [&](const std::vector<int> &v) {
+    s += "[";
+    for (size_t i = 0; i < v.size(); ++i) {
+      if (i) s += ",";
+      s += std::to_string(v[i]);
+    }
+    s += "]";
+  };
+  auto cplx = [&](const std::vector<cd> &v) {
+    s += "[";
+    for (size_t i = 0; i < v.size(); ++i) {
+      if (i) s += ",";
+      s += "[";
+      num(v[i].real());
+      s += ",";
+      num(v[i].imag());
+      s += "]";
+    }
+    s += "]";
+  };
+  auto i64s = [&](const std::vector<int64_t> &v) {
+    std::vector<int> w(v.begin(), v.end());
+    ints(w);
+  };
+  s += "{\"nq\":" + std::to_string(pl.nq) + ",\"passes\":[";
+  for (size_t i = 0; i < pl.passes.size(); ++i) {
+    const Pass &ps = pl.passes[i];
+    if (i) s += ",";
+    if (ps.kind == Pass::DENSE || ps.kind == Pass::PERM) {
+      s += ps.kind == Pass::DENSE ? "{\"kind\":\"dense\",\"qubits\":" : "{\"kind\":\"perm\",\"qubits\":";
+      ints(ps.op.q);
+      if (ps.kind == Pass::DENSE) {
+        s += ",\"matrix\":";
+        cplx(ps.op.m);
+      } else {
+        s += ",\"perm\":";
+        i64s(ps.op.perm);
+      }
+      s += "}";
+    } else if (ps.kind == Pass::DIAG) {
+      s += "{\"kind\":\"diag\",\"tables\":[";
+      for (size_t t = 0; t < ps.tq.size(); ++t) {
+        if (t) s += ",";
+        s += "{\"qubits\":";
+        ints(ps.tq[t]);
+        s += ",\"table\":";
+        cplx(ps.tables[t]);
+        s += "}";
+      }
+      s += "]}";
+    } else {
+      s += "{\"kind\":\"tile\",\"t\":" + std::to_string(ps.t) + ",\"L\":" + std::to_string(ps.L) +
+           ",\"E\":";
+      ints(ps.E);
+      s += ",\"ops\":[";
+      for (size_t o = 0; o < ps.tops.size(); ++o) {
+        const TileOpHost &th = ps.tops[o];
+        if (o) s += ",";
+        s += std::string("{\"kind\":\"") +
+             (th.kind == OP_DENSE ? "dense" : th.kind == OP_DIAG ? "diag" : "perm") +
+             "\",\"pos\":";
+        ints(th.pos);
+        if (th.kind == OP_PERM) {
+          s += ",\"perm\":";
+          i64s(th.perm);
+        } else {
+          s += ",\"data\":";
+          cplx(th.data);
+        }
+        s += "}";
+      }
+      s += "]}";
+    }
+  }
+  s += "]}";
+  return s;
+}
+
+static int program_max_qubit(qvmg_program p) {
+  int m = 0;
+  for (auto &op : p->ops)
+    for (int q : op.q) m = std::max(m, q + 1);
+  return m;
+}
+
+}  // namespace qvmg
+
+using namespace qvmg;
+
+extern "C" {
+
+int qvmg_program_create(qvmg_program *out) {
+  if (!out) return fail(QVMG_E_INVALID, "null output handle");
+  *out = new qvmg_program_s();
+  return QVMG_OK;
+}
+
+int qvmg_program_free(qvmg_program p) {
+  delete p;
+  return QVMG_OK;
+}
+
+int qvmg_program_add_dense(qvmg_program p, int k, const int *qubits, const double *matrix) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  int rc = check_op_qubits(k, qubits, QVMG_MAX_GATE_QUBITS);
+  if (rc) return rc;
+  if (!matrix) return fail(QVMG_E_INVALID, "null matrix");
+  Op op;
+  op.kind = OP_DENSE;
+  op.q.assign(qubits, qubits + k);
+  int d = 1 << k;
+  op.m.resize((size_t)d * d);
+  for (int i = 0; i < d * d; ++i) op.m[i] = cd(matrix[2 * i], matrix[2 * i + 1]);
+  std::lock_guard<std::mutex> g(p->mu);
+  p->ops.push_back(std::move(op));
+  p->plans.clear();
+  return QVMG_OK;
+}
+
+int qvmg_program_add_permutation(qvmg_program p, int k, const int *qubits, const int64_t *perm) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  int rc = check_op_qubits(k, qubits, QVMG_MAX_GATE_QUBITS);
+  if (rc) return rc;
+  if (!perm) return fail(QVMG_E_INVALID, "null permutation");
+  int d = 1 << k;
+  std::vector<int> seen(d, 0);
+  for (int j = 0; j < d; ++j) {
+    if (perm[j] < 0 || perm[j] >= d || seen[perm[j]])
+      return fail(QVMG_E_INVALID, "not a permutation of 0..2^k-1");
+    seen[perm[j]] = 1;
+  }
+  Op op;
+  op.kind = OP_PERM;
+  op.q.assign(qubits, qubits + k);
+  op.perm.assign(perm, perm + d);
+  std::lock_guard<std::mutex> g(p->mu);
+  p->ops.push_back(std::move(op));
+  p->plans.clear();
+  return QVMG_OK;
+}
+
+int qvmg_program_add_diagonal(qvmg_program p, int k, const int *qubits, const double *diag) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  int rc = check_op_qubits(k, qubits, QVMG_MAX_DIAG_QUBITS);
+  if (rc) return rc;
+  if (!diag) return fail(QVMG_E_INVALID, "null diagonal");
+  Op op;
+  op.kind = OP_DIAG;
+  op.q.assign(qubits, qubits + k);
+  int d = 1 << k;
+  op.m.resize(d);
+  for (int i = 0; i < d; ++i) op.m[i] = cd(diag[2 * i], diag[2 * i + 1]);
+  std::lock_guard<std::mutex> g(p->mu);
+  p->ops.push_back(std::move(op));
+  p->plans.clear();
+  return QVMG_OK;
+}
+
+int qvmg_program_num_ops(qvmg_program p, int *nops) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  if (nops) *nops = (int)p->ops.size();
+  return QVMG_OK;
+}
+
+int qvmg_program_plan(qvmg_program p, int nqubits, int precision, int mode, int fusion_width,
+                      int tile_qubits, int *npasses) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  if (nqubits < 1 || nqubits > QVMG_MAX_QUBITS) return fail(QVMG_E_INVALID, "bad qubit count");
+  if (precision != QVMG_FP64 && precision != QVMG_FP32)
+    return fail(QVMG_E_INVALID, "bad precision");
+  if (mode != QVMG_RUN_PLAIN && mode != QVMG_RUN_FUSED) return fail(QVMG_E_INVALID, "bad mode");
+  if (fusion_width < 1 || fusion_width > QVMG_MAX_GATE_QUBITS)
+    return fail(QVMG_E_INVALID, "fusion width must be 1..5");
+  if (tile_qubits < 0 || tile_qubits > 16) return fail(QVMG_E_INVALID, "tile width must be 0..16");
+  std::lock_guard<std::mutex> g(p->mu);
+  if (program_max_qubit(p) > nqubits)
+    return fail(QVMG_E_INVALID, "program uses a qubit beyond the state's qubit count");
+  make_plan(p->ops, nqubits, precision, mode, fusion_width, tile_qubits, p->last_plan);
+  p->default_fw = fusion_width;
+  p->default_tile = tile_qubits;
+  if (npasses) *npasses = (int)p->last_plan.passes.size();
+  return QVMG_OK;
+}
+
+int qvmg_program_plan_stats(qvmg_program p, int64_t *stats, int nstats) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  const Plan &pl = p->last_plan;
+  int64_t state_bytes = pl.nq > 0 ? ((int64_t)1 << pl.nq) * (pl.prec == QVMG_FP64 ? 16 : 8) : 0;
+  // bytes a run uploads when it builds its device plan
+  int64_t csz = pl.prec == QVMG_FP64 ? 16 : 8, up = 0;
+  for (const Pass &ps : pl.passes) {
+    if (ps.kind == Pass::DIAG)
+      for (auto &t : ps.tables) up += csz * (int64_t)t.size();
+    if (ps.kind == Pass::TILE)
+      for (auto &o : ps.tops) up += csz * (int64_t)o.data.size() + (int64_t)sizeof(TileOpDev);
+  }
+  int64_t v[8] = {pl.n_src, (int64_t)pl.passes.size(), pl.n_tile, pl.n_blocks, pl.n_diag,
+                  pl.n_perm, 2 * state_bytes * (int64_t)pl.passes.size(), up};
+  for (int i = 0; i < nstats && i < 8; ++i) stats[i] = v[i];
+  return QVMG_OK;
+}
+
+int qvmg_program_plan_describe(qvmg_program p, char *buf, uint64_t cap, uint64_t *needed) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  std::string js = describe_plan(p->last_plan);
+  if (needed) *needed = js.size() + 1;
+  if (buf && cap > 0) {
+    size_t n = std::min<size_t>(cap - 1, js.size());
+    std::memcpy(buf, js.data(), n);
+    buf[n] = 0;
+    if (n < js.size()) return fail(QVMG_E_INVALID, "buffer too small for the plan description");
+  }
+  return QVMG_OK;
+}
+
+// Find or build the device plan of `p` for state `s` (caller holds p->mu).
+static int device_plan_for(qvmg_state s, qvmg_program p, int mode, DevicePlan **out) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  if (mode != QVMG_RUN_PLAIN && mode != QVMG_RUN_FUSED) return fail(QVMG_E_INVALID, "bad mode");
+  if (program_max_qubit(p) > s->nq)
+    return fail(QVMG_E_INVALID, "program uses a qubit beyond the state's qubit count");
+  int fw = mode == QVMG_RUN_FUSED ? p->default_fw : 1;
+  int tile = mode == QVMG_RUN_FUSED ? p->default_tile : 0;
+  auto key = std::make_tuple(s->nq, s->prec, mode, fw, tile);
+  auto it = p->plans.find(key);
+  if (it == p->plans.end()) {
+    auto dp = std::make_unique<DevicePlan>();
+    if ((rc = build_device_plan(p, s->nq, s->prec, mode, fw, tile, *dp))) return rc;
+    it = p->plans.emplace(key, std::move(dp)).first;
+  }
+  *out = it->second.get();
+  return QVMG_OK;
+}
+
+int qvmg_program_run(qvmg_state s, qvmg_program p, int mode) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  std::lock_guard<std::mutex> g(p->mu);
+  DevicePlan *dp = nullptr;
+  int rc = device_plan_for(s, p, mode, &dp);
+  if (rc) return rc;
+  return run_device_plan(s, *dp);
+}
+
+int qvmg_program_run_profiled(qvmg_state s, qvmg_program p, int mode, float *pass_ms,
+                              int *pass_kind, int cap, int *npasses) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  std::lock_guard<std::mutex> g(p->mu);
+  DevicePlan *dp = nullptr;
+  int rc = device_plan_for(s, p, mode, &dp);
+  if (rc) return rc;
+  size_t np = dp->plan.passes.size();
+  std::vector<cudaEvent_t> ev(np + 1);
+  for (auto &e : ev) QVMG_CUDA(cudaEventCreate(&e));
+  rc = run_device_plan(s, *dp, ev.data());
+  if (rc == QVMG_OK) {
+    cudaError_t e = cudaEventSynchronize(ev[np]);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventSynchronize");
+  }
+  if (rc == QVMG_OK) {
+    for (size_t i = 0; i < np && (int)i < cap; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+      if (pass_ms) pass_ms[i] = ms;
+      if (pass_kind) pass_kind[i] = (int)dp->plan.passes[i].kind;
+    }
+    if (npasses) *npasses = (int)np;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+int qvmg_state_stream(qvmg_state s, void **stream) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if (stream) *stream = (void *)s->stream;
+  return QVMG_OK;
+}
+
+}  // extern "C"

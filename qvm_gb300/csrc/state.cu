@@ -1,0 +1,354 @@
+// state.cu -- library-wide plumbing and the pure-state lifecycle.
+//
+// A qvmg_state owns 2^n amplitudes in HBM (double2 or float2, LSB-first
+// index) plus small reduction scratch, and its own CUDA stream.  This file
+// replaces make-pure-state / allocate-vector / bring-to-zero-state /
+// copy-wavefunction of the reference (src/state-representation.lisp:76-152,
+// src/allocator.lisp:47-106, src/wavefunction.lisp:80-109).
+#include <cuda_runtime.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "internal.h"
+
+namespace qvmg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? QVMG_E_NOMEM : QVMG_E_CUDA;
+}
+
+static int g_sm_count = 0;
+static std::once_flag g_sm_once;
+
+int sm_count() {
+  std::call_once(g_sm_once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sm_count <= 0) g_sm_count = 1;
+  });
+  return g_sm_count;
+}
+
+int grid_for(uint64_t work, int threads, int per_sm) {
+  uint64_t need = (work + threads - 1) / threads;
+  uint64_t cap = (uint64_t)sm_count() * per_sm;
+  uint64_t g = std::min<uint64_t>(need, cap);
+  return (int)std::max<uint64_t>(g, 1);
+}
+
+int check_state(qvmg_state s) {
+  if (!s || !s->amps) return fail(QVMG_E_INVALID, "null or freed state handle");
+  return QVMG_OK;
+}
+
+int check_qubits(qvmg_state s, int k, const int *qubits, int kmax) {
+  if (k < 1 || k > kmax)
+    return fail(QVMG_E_INVALID, "gate width k=" + std::to_string(k) + " outside 1.." +
+                                    std::to_string(kmax));
+  if (k > s->nq)
+    return fail(QVMG_E_INVALID, "gate on " + std::to_string(k) + " qubits applied to a " +
+                                    std::to_string(s->nq) + "-qubit state");
+  if (!qubits) return fail(QVMG_E_INVALID, "null qubit tuple");
+  for (int i = 0; i < k; ++i) {
+    if (qubits[i] < 0 || qubits[i] >= s->nq)
+      return fail(QVMG_E_INVALID, "qubit " + std::to_string(qubits[i]) +
+                                      " out of range for a " + std::to_string(s->nq) +
+                                      "-qubit state");
+    for (int j = 0; j < i; ++j)
+      if (qubits[j] == qubits[i])
+        return fail(QVMG_E_INVALID, "repeated qubit " + std::to_string(qubits[i]));
+  }
+  return QVMG_OK;
+}
+
+int ensure_dvec(qvmg_state s, uint64_t bytes) {
+  if (s->dvec_bytes >= bytes) return QVMG_OK;
+  if (s->dvec) {
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFree(s->dvec);
+    s->dvec = nullptr;
+    s->dvec_bytes = 0;
+  }
+  uint64_t want = std::max<uint64_t>(bytes, 1 << 16);
+  QVMG_CUDA(cudaMalloc(&s->dvec, want));
+  s->dvec_bytes = want;
+  return QVMG_OK;
+}
+
+int ensure_staging(qvmg_state s, uint64_t bytes) {
+  if (s->staging_bytes >= bytes) return QVMG_OK;
+  if (s->staging) {
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFree(s->staging);
+    s->staging = nullptr;
+    s->staging_bytes = 0;
+  }
+  QVMG_CUDA(cudaMalloc(&s->staging, bytes));
+  s->staging_bytes = bytes;
+  return QVMG_OK;
+}
+
+int ensure_pinned(qvmg_state s, uint64_t bytes) {
+  if (s->pinned_bytes >= bytes) return QVMG_OK;
+  if (s->pinned) {
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFreeHost(s->pinned);
+    s->pinned = nullptr;
+    s->pinned_bytes = 0;
+  }
+  QVMG_CUDA(cudaMallocHost(&s->pinned, bytes));
+  s->pinned_bytes = bytes;
+  return QVMG_OK;
+}
+
+// ---- kernels -------------------------------------------------------------------
+__global__ void k_set_amp0(void *amps, int prec) {
+  if (prec == QVMG_FP64)
+    ((double2 *)amps)[0] = make_double2(1.0, 0.0);
+  else
+    ((float2 *)amps)[0] = make_float2(1.0f, 0.0f);
+}
+
+__global__ void k_f64_to_f32(const double2 *__restrict__ in, float2 *__restrict__ out,
+                             uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    double2 v = in[i];
+    out[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+__global__ void k_f32_to_f64(const float2 *__restrict__ in, double2 *__restrict__ out,
+                             uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    float2 v = in[i];
+    out[i] = make_double2((double)v.x, (double)v.y);
+  }
+}
+
+static int order_after(qvmg_state waiter, qvmg_state producer) {
+  if (waiter->stream == producer->stream) return QVMG_OK;
+  cudaEvent_t ev;
+  QVMG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e1 = cudaEventRecord(ev, producer->stream);
+  cudaError_t e2 = cudaStreamWaitEvent(waiter->stream, ev, 0);
+  cudaEventDestroy(ev);
+  if (e1 != cudaSuccess) return cuda_fail(e1, "cudaEventRecord");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamWaitEvent");
+  return QVMG_OK;
+}
+
+int order_states(qvmg_state waiter, qvmg_state producer) { return order_after(waiter, producer); }
+
+}  // namespace qvmg
+
+using namespace qvmg;
+
+extern "C" {
+
+const char *qvmg_last_error(void) { return g_last_error.c_str(); }
+
+int qvmg_abi_version(void) { return QVMG_ABI_VERSION; }
+
+int qvmg_device_info(int *sms, uint64_t *free_bytes, uint64_t *total_bytes) {
+  size_t f = 0, t = 0;
+  QVMG_CUDA(cudaMemGetInfo(&f, &t));
+  if (sms) *sms = sm_count();
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return QVMG_OK;
+}
+
+uint64_t qvmg_state_bytes(int nqubits, int precision) {
+  if (nqubits < 1 || nqubits > QVMG_MAX_QUBITS) return 0;
+  if (precision != QVMG_FP64 && precision != QVMG_FP32) return 0;
+  uint64_t len = 1ull << nqubits;
+  uint64_t nblocks = nqubits > kSampleBlockBits ? (len >> kSampleBlockBits) : 1;
+  return len * amp_bytes(precision) + (nblocks + 1) * sizeof(double) +
+         2 * kReduceBlocks * sizeof(double) + sizeof(MeasResult);
+}
+
+int qvmg_state_create(int nqubits, int precision, qvmg_state *out) {
+  if (!out) return fail(QVMG_E_INVALID, "null output handle");
+  *out = nullptr;
+  if (nqubits < 1 || nqubits > QVMG_MAX_QUBITS)
+    return fail(QVMG_E_INVALID, "qubit count " + std::to_string(nqubits) + " outside 1.." +
+                                    std::to_string(QVMG_MAX_QUBITS));
+  if (precision != QVMG_FP64 && precision != QVMG_FP32)
+    return fail(QVMG_E_INVALID, "precision must be QVMG_FP64 or QVMG_FP32");
+  qvmg_state s = new qvmg_state_s();
+  s->nq = nqubits;
+  s->prec = precision;
+  s->len = 1ull << nqubits;
+  s->nblocks = nqubits > kSampleBlockBits ? (s->len >> kSampleBlockBits) : 1;
+  cudaGetDevice(&s->device);
+  int rc = QVMG_OK;
+  cudaError_t e;
+  do {
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+      rc = cuda_fail(e, "cudaStreamCreate");
+      break;
+    }
+    if ((e = cudaMalloc(&s->amps, s->len * amp_bytes(precision))) != cudaSuccess) {
+      rc = cuda_fail(e, "cudaMalloc(amplitudes)");
+      break;
+    }
+    if ((e = cudaMalloc(&s->partials, 2 * kReduceBlocks * sizeof(double))) != cudaSuccess) {
+      rc = cuda_fail(e, "cudaMalloc(partials)");
+      break;
+    }
+    if ((e = cudaMalloc(&s->block_sums, (s->nblocks + 1) * sizeof(double))) != cudaSuccess) {
+      rc = cuda_fail(e, "cudaMalloc(block sums)");
+      break;
+    }
+    if ((e = cudaMalloc(&s->dres, sizeof(MeasResult))) != cudaSuccess) {
+      rc = cuda_fail(e, "cudaMalloc(result)");
+      break;
+    }
+    if ((e = cudaMallocHost(&s->hres, sizeof(MeasResult))) != cudaSuccess) {
+      rc = cuda_fail(e, "cudaMallocHost(result)");
+      break;
+    }
+  } while (0);
+  if (rc == QVMG_OK) rc = qvmg_state_reset(s);
+  if (rc != QVMG_OK) {
+    std::string msg = g_last_error;
+    qvmg_state_free(s);
+    g_last_error = msg;
+    return rc;
+  }
+  *out = s;
+  return QVMG_OK;
+}
+
+int qvmg_state_free(qvmg_state s) {
+  if (!s) return QVMG_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->amps) cudaFree(s->amps);
+  if (s->partials) cudaFree(s->partials);
+  if (s->block_sums) cudaFree(s->block_sums);
+  if (s->dres) cudaFree(s->dres);
+  if (s->hres) cudaFreeHost(s->hres);
+  if (s->staging) cudaFree(s->staging);
+  if (s->pinned) cudaFreeHost(s->pinned);
+  if (s->dvec) cudaFree(s->dvec);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  s->amps = nullptr;
+  delete s;
+  return QVMG_OK;
+}
+
+int qvmg_state_info(qvmg_state s, int *nqubits, int *precision) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if (nqubits) *nqubits = s->nq;
+  if (precision) *precision = s->prec;
+  return QVMG_OK;
+}
+
+int qvmg_state_reset(qvmg_state s) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  QVMG_CUDA(cudaMemsetAsync(s->amps, 0, s->len * amp_bytes(s->prec), s->stream));
+  k_set_amp0<<<1, 1, 0, s->stream>>>(s->amps, s->prec);
+  QVMG_CHECK_LAUNCH("k_set_amp0");
+  return QVMG_OK;
+}
+
+// Chunk size for precision-converting transfers (in amplitudes).
+static const uint64_t kChunk = 1ull << 22;
+
+int qvmg_state_upload(qvmg_state s, const double *amps) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if (!amps) return fail(QVMG_E_INVALID, "null host buffer");
+  if (s->prec == QVMG_FP64) {
+    QVMG_CUDA(cudaMemcpyAsync(s->amps, amps, s->len * 16, cudaMemcpyHostToDevice, s->stream));
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+    return QVMG_OK;
+  }
+  uint64_t chunk = std::min(kChunk, s->len);
+  if ((rc = ensure_staging(s, chunk * 16))) return rc;
+  for (uint64_t off = 0; off < s->len; off += chunk) {
+    uint64_t n = std::min(chunk, s->len - off);
+    QVMG_CUDA(cudaMemcpyAsync(s->staging, amps + 2 * off, n * 16, cudaMemcpyHostToDevice,
+                              s->stream));
+    k_f64_to_f32<<<grid_for(n, 256), 256, 0, s->stream>>>((const double2 *)s->staging,
+                                                          (float2 *)s->amps + off, n);
+    QVMG_CHECK_LAUNCH("k_f64_to_f32");
+  }
+  QVMG_CUDA(cudaStreamSynchronize(s->stream));
+  return QVMG_OK;
+}
+
+int qvmg_state_download(qvmg_state s, double *amps) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if (!amps) return fail(QVMG_E_INVALID, "null host buffer");
+  if (s->prec == QVMG_FP64) {
+    QVMG_CUDA(cudaMemcpyAsync(amps, s->amps, s->len * 16, cudaMemcpyDeviceToHost, s->stream));
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+    return QVMG_OK;
+  }
+  uint64_t chunk = std::min(kChunk, s->len);
+  if ((rc = ensure_staging(s, chunk * 16))) return rc;
+  for (uint64_t off = 0; off < s->len; off += chunk) {
+    uint64_t n = std::min(chunk, s->len - off);
+    k_f32_to_f64<<<grid_for(n, 256), 256, 0, s->stream>>>((const float2 *)s->amps + off,
+                                                          (double2 *)s->staging, n);
+    QVMG_CHECK_LAUNCH("k_f32_to_f64");
+    QVMG_CUDA(cudaMemcpyAsync(amps + 2 * off, s->staging, n * 16, cudaMemcpyDeviceToHost,
+                              s->stream));
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  return QVMG_OK;
+}
+
+int qvmg_state_copy(qvmg_state dst, qvmg_state src) {
+  int rc = check_state(dst);
+  if (rc) return rc;
+  if ((rc = check_state(src))) return rc;
+  if (dst->nq != src->nq)
+    return fail(QVMG_E_INVALID, "copy between states of different qubit counts");
+  if (dst == src) return QVMG_OK;
+  if ((rc = order_after(dst, src))) return rc;
+  if (dst->prec == src->prec) {
+    QVMG_CUDA(cudaMemcpyAsync(dst->amps, src->amps, dst->len * amp_bytes(dst->prec),
+                              cudaMemcpyDeviceToDevice, dst->stream));
+  } else if (src->prec == QVMG_FP64) {
+    k_f64_to_f32<<<grid_for(dst->len, 256), 256, 0, dst->stream>>>(
+        (const double2 *)src->amps, (float2 *)dst->amps, dst->len);
+    QVMG_CHECK_LAUNCH("k_f64_to_f32");
+  } else {
+    k_f32_to_f64<<<grid_for(dst->len, 256), 256, 0, dst->stream>>>(
+        (const float2 *)src->amps, (double2 *)dst->amps, dst->len);
+    QVMG_CHECK_LAUNCH("k_f32_to_f64");
+  }
+  // The source must not be modified before the copy has read it.
+  return order_after(src, dst);
+}
+
+int qvmg_state_sync(qvmg_state s) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  QVMG_CUDA(cudaStreamSynchronize(s->stream));
+  return QVMG_OK;
+}
+
+}  // extern "C"

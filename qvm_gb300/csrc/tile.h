@@ -1,0 +1,38 @@
+// tile.h -- device descriptors of a shared-memory tile pass.
+#pragma once
+#include <stdint.h>
+
+#include "internal.h"
+
+namespace qvmg {
+
+constexpr int kTileThreads = 512;
+constexpr int kTileMaxSmem = 227 * 1024;
+constexpr int kTileMaxE = 24;
+
+// One op of a tile pass (128 bytes, copied into shared memory as words).
+struct TileOpDev {
+  int kind;  // 0 dense, 1 diagonal table, 2 permutation
+  int k;     // qubits
+  int data;  // offset (complex elements) of the matrix / table in pass data
+  int nmoved;
+  int pos[10];  // dense/perm: tile-local bit positions; diag: global qubits (nat order)
+  unsigned char src[32];
+  unsigned char dst[32];
+};
+static_assert(sizeof(TileOpDev) == 120, "TileOpDev layout");
+
+struct TileArgs {
+  int t, L, nE, nops;
+  int E[kTileMaxE];  // global qubit of tile bit L+e, ascending
+  int ndata;         // complex elements of op data
+  int kmax;          // widest dense/permutation op of the pass (1..5)
+  unsigned long long ntiles;
+  const void *ops;   // TileOpDev[nops] in device memory
+  const void *data;  // complex op data in device memory (state precision)
+};
+
+size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops);
+int launch_tile(qvmg_state s, const TileArgs &args);
+
+}  // namespace qvmg

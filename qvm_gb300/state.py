@@ -1,0 +1,266 @@
+"""Device-resident pure state and gate programs over the C ABI.
+
+``CudaPureState`` mirrors the reference's state protocol on ``pure-state``
+(src/state-representation.lisp:25-168): ``num_qubits``,
+``set_to_zero_state``, ``state_elements`` / ``set_state_elements`` (the
+amplitudes, downloaded/uploaded as complex128, LSB-first), plus the
+measurement protocol of src/measurement.lisp.  The amplitudes never leave
+HBM unless ``state_elements`` is called.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+PRECISIONS = {"fp64": L.FP64, "fp32": L.FP32, L.FP64: L.FP64, L.FP32: L.FP32}
+
+
+def _qubit_array(qubits):
+    return (ctypes.c_int * len(qubits))(*[int(q) for q in qubits])
+
+
+def _cplx(arr) -> np.ndarray:
+    return np.ascontiguousarray(arr, dtype=np.complex128)
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def state_bytes(nqubits: int, precision="fp64") -> int:
+    """HBM bytes a state of this size needs (admission control)."""
+    return int(L.lib().qvmg_state_bytes(int(nqubits), PRECISIONS[precision]))
+
+
+def device_info():
+    sms = ctypes.c_int(0)
+    free = ctypes.c_uint64(0)
+    total = ctypes.c_uint64(0)
+    L.call("qvmg_device_info", ctypes.byref(sms), ctypes.byref(free), ctypes.byref(total))
+    return {"sm_count": sms.value, "free_bytes": free.value, "total_bytes": total.value}
+
+
+class CudaPureState:
+    """A pure state of ``num_qubits`` qubits held in GPU memory."""
+
+    def __init__(self, num_qubits: int, precision="fp64"):
+        self._h = ctypes.c_void_p()
+        self.precision = PRECISIONS[precision]
+        L.call("qvmg_state_create", int(num_qubits), self.precision, ctypes.byref(self._h))
+        self._n = int(num_qubits)
+
+    # -- lifecycle ----------------------------------------------------------
+    @property
+    def handle(self):
+        if not self._h:
+            raise ValueError("state has been freed")
+        return self._h
+
+    def free(self):
+        if self._h:
+            L.call("qvmg_state_free", self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    # -- state protocol ------------------------------------------------------
+    def num_qubits(self) -> int:
+        return self._n
+
+    def set_to_zero_state(self):
+        L.call("qvmg_state_reset", self.handle)
+
+    def state_elements(self) -> np.ndarray:
+        out = np.empty(1 << self._n, dtype=np.complex128)
+        L.call("qvmg_state_download", self.handle, _dptr(out))
+        return out
+
+    def set_state_elements(self, amps):
+        a = _cplx(amps)
+        if a.shape != (1 << self._n,):
+            raise ValueError(f"expected {1 << self._n} amplitudes, got {a.shape}")
+        L.call("qvmg_state_upload", self.handle, _dptr(a))
+
+    def copy_from(self, other: "CudaPureState"):
+        L.call("qvmg_state_copy", self.handle, other.handle)
+
+    def sync(self):
+        L.call("qvmg_state_sync", self.handle)
+
+    def stream(self) -> int:
+        """The state's cudaStream_t as an integer (for events / ordering)."""
+        p = ctypes.c_void_p()
+        L.call("qvmg_state_stream", self.handle, ctypes.byref(p))
+        return int(p.value or 0)
+
+    # -- gates -----------------------------------------------------------------
+    def apply_matrix(self, matrix, qubits):
+        """apply-matrix-operator: ``qubits`` is a nat-tuple (qubits[0] is
+        the matrix LSB, i.e. the last Quil argument)."""
+        m = _cplx(matrix)
+        L.call("qvmg_apply_dense", self.handle, len(qubits), _qubit_array(qubits), _dptr(m))
+
+    def apply_permutation(self, perm, qubits):
+        p = np.ascontiguousarray(perm, dtype=np.int64)
+        L.call("qvmg_apply_permutation", self.handle, len(qubits), _qubit_array(qubits),
+               p.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+
+    def apply_diagonal(self, diag, qubits):
+        d = _cplx(diag)
+        L.call("qvmg_apply_diagonal", self.handle, len(qubits), _qubit_array(qubits), _dptr(d))
+
+    # -- measurement -------------------------------------------------------------
+    def excited_probability(self, q: int) -> float:
+        p = ctypes.c_double()
+        L.call("qvmg_prob_excited", self.handle, int(q), ctypes.byref(p))
+        return p.value
+
+    def ground_probability(self, q: int) -> float:
+        p = ctypes.c_double()
+        L.call("qvmg_prob_ground", self.handle, int(q), ctypes.byref(p))
+        return p.value
+
+    def force_measurement(self, measured_value: int, q: int, excited_probability: float):
+        L.call("qvmg_force_measurement", self.handle, int(q), int(measured_value),
+               float(excited_probability))
+
+    def measure(self, q: int, draw: float, compiled: bool = False):
+        """Returns (bit, draw_used, probability)."""
+        bit = ctypes.c_int()
+        used = ctypes.c_int()
+        prob = ctypes.c_double()
+        conv = L.MEASURE_COMPILED if compiled else L.MEASURE_INTERPRETED
+        L.call("qvmg_measure", self.handle, int(q), float(draw), conv, ctypes.byref(bit),
+               ctypes.byref(used), ctypes.byref(prob))
+        return bit.value, bool(used.value), prob.value
+
+    def measure_all(self, draw: float) -> int:
+        idx = ctypes.c_uint64()
+        L.call("qvmg_measure_all", self.handle, float(draw), ctypes.byref(idx))
+        return int(idx.value)
+
+    def sample(self, draws, rule: str = "bisect") -> np.ndarray:
+        d = np.ascontiguousarray(draws, dtype=np.float64)
+        out = np.zeros(len(d), dtype=np.uint64)
+        r = L.SAMPLE_BISECT if rule == "bisect" else L.SAMPLE_CDF
+        L.call("qvmg_sample", self.handle, _dptr(d), len(d), r,
+               out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+        return out
+
+    def probabilities(self) -> np.ndarray:
+        out = np.empty(1 << self._n, dtype=np.float64)
+        L.call("qvmg_probabilities", self.handle, _dptr(out))
+        return out
+
+    def norm(self) -> float:
+        n = ctypes.c_double()
+        L.call("qvmg_norm", self.handle, ctypes.byref(n))
+        return n.value
+
+    def normalize(self):
+        L.call("qvmg_normalize", self.handle)
+
+    def inner(self, other: "CudaPureState") -> complex:
+        re = ctypes.c_double()
+        im = ctypes.c_double()
+        L.call("qvmg_inner", self.handle, other.handle, ctypes.byref(re), ctypes.byref(im))
+        return complex(re.value, im.value)
+
+    def fidelity(self, other: "CudaPureState"):
+        """(|<self|other>|^2, max |self_i - other_i|)."""
+        f = ctypes.c_double()
+        e = ctypes.c_double()
+        L.call("qvmg_fidelity", self.handle, other.handle, ctypes.byref(f), ctypes.byref(e))
+        return f.value, e.value
+
+
+class Program:
+    """A list of gate ops run on a state in plain or fused mode."""
+
+    def __init__(self):
+        self._h = ctypes.c_void_p()
+        L.call("qvmg_program_create", ctypes.byref(self._h))
+
+    def free(self):
+        if self._h:
+            L.call("qvmg_program_free", self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def add_dense(self, matrix, qubits):
+        m = _cplx(matrix)
+        L.call("qvmg_program_add_dense", self._h, len(qubits), _qubit_array(qubits), _dptr(m))
+
+    def add_permutation(self, perm, qubits):
+        p = np.ascontiguousarray(perm, dtype=np.int64)
+        L.call("qvmg_program_add_permutation", self._h, len(qubits), _qubit_array(qubits),
+               p.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+
+    def add_diagonal(self, diag, qubits):
+        d = _cplx(diag)
+        L.call("qvmg_program_add_diagonal", self._h, len(qubits), _qubit_array(qubits), _dptr(d))
+
+    def add_gates(self, gates):
+        """Add (matrix, nat-tuple qubits) pairs as dense ops."""
+        for m, qs in gates:
+            self.add_dense(m, qs)
+        return self
+
+    def num_ops(self) -> int:
+        n = ctypes.c_int()
+        L.call("qvmg_program_num_ops", self._h, ctypes.byref(n))
+        return n.value
+
+    def plan(self, nqubits: int, precision="fp64", fused: bool = True, fusion_width: int = 2,
+             tile_qubits: int = 0) -> dict:
+        """Plan on the host (no GPU work) and return the plan statistics."""
+        npasses = ctypes.c_int()
+        L.call("qvmg_program_plan", self._h, int(nqubits), PRECISIONS[precision],
+               L.RUN_FUSED if fused else L.RUN_PLAIN, int(fusion_width), int(tile_qubits),
+               ctypes.byref(npasses))
+        st = (ctypes.c_int64 * 8)()
+        L.call("qvmg_program_plan_stats", self._h, st, 8)
+        keys = ["source_ops", "passes", "tile_passes", "fused_blocks", "diag_passes",
+                "perm_passes", "bytes_moved", "upload_bytes"]
+        return dict(zip(keys, [int(x) for x in st]))
+
+    def describe(self) -> dict:
+        """The last plan's passes as a dict (see qvmg_program_plan_describe)."""
+        import json
+        need = ctypes.c_uint64()
+        L.call("qvmg_program_plan_describe", self._h, None, 0, ctypes.byref(need))
+        buf = ctypes.create_string_buffer(need.value)
+        L.call("qvmg_program_plan_describe", self._h, buf, need.value, ctypes.byref(need))
+        return json.loads(buf.value.decode())
+
+    def run(self, state: CudaPureState, fused: bool = True):
+        L.call("qvmg_program_run", state.handle, self._h, L.RUN_FUSED if fused else L.RUN_PLAIN)
+
+    def run_profiled(self, state: CudaPureState, fused: bool = True, cap: int = 1 << 16):
+        """Run with an event around every pass; returns (ms[], kinds[]) with
+        kinds 0 dense, 1 diagonal, 2 permutation, 3 tile."""
+        ms = (ctypes.c_float * cap)()
+        kinds = (ctypes.c_int * cap)()
+        n = ctypes.c_int()
+        L.call("qvmg_program_run_profiled", state.handle, self._h,
+               L.RUN_FUSED if fused else L.RUN_PLAIN, ms, kinds, cap, ctypes.byref(n))
+        k = min(n.value, cap)
+        return np.array(ms[:k], dtype=np.float64), np.array(kinds[:k], dtype=np.int32)

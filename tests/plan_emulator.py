@@ -1,0 +1,45 @@
+"""Execute a plan description (qvmg_program_plan_describe) on the CPU with the
+oracle, to check the planner's fusion and tiling logic without a GPU.
+
+Test infrastructure: the library itself never executes plans on the CPU.
+"""
+import numpy as np
+
+
+def _cplx(pairs):
+    a = np.array(pairs, dtype=np.float64).reshape(-1, 2)
+    return a[:, 0] + 1j * a[:, 1]
+
+
+def _apply_table(wf, qubits, table):
+    idx = np.arange(len(wf), dtype=np.int64)
+    sub = np.zeros(len(wf), dtype=np.int64)
+    for j, q in enumerate(qubits):
+        sub |= ((idx >> q) & 1) << j
+    wf *= table[sub]
+
+
+def run_description(oracle, desc, wf):
+    for p in desc["passes"]:
+        kind = p["kind"]
+        if kind == "dense":
+            d = 1 << len(p["qubits"])
+            oracle.apply_matrix_operator(wf, _cplx(p["matrix"]).reshape(d, d), p["qubits"])
+        elif kind == "perm":
+            oracle.apply_permutation(wf, p["perm"], p["qubits"])
+        elif kind == "diag":
+            for t in p["tables"]:
+                _apply_table(wf, t["qubits"], _cplx(t["table"]))
+        else:
+            L, E = p["L"], p["E"]
+            glob = lambda pos: pos if pos < L else E[pos - L]  # noqa: E731
+            for op in p["ops"]:
+                if op["kind"] == "diag":
+                    _apply_table(wf, op["pos"], _cplx(op["data"]))
+                elif op["kind"] == "perm":
+                    oracle.apply_permutation(wf, op["perm"], [glob(x) for x in op["pos"]])
+                else:
+                    k = len(op["pos"])
+                    m = _cplx(op["data"]).reshape(1 << k, 1 << k)
+                    oracle.apply_matrix_operator(wf, m, [glob(x) for x in op["pos"]])
+    return wf

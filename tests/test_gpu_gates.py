@@ -1,0 +1,222 @@
+"""GPU parity: per-gate kernels and programs against the CPU oracle.
+
+FP64 results must match the oracle within 1e-12 (absolute, per amplitude);
+FP32 within 2e-6 absolute per amplitude on normalised states and fidelity
+>= 1 - 1e-6.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from qvm_gb300 import CudaPureState, Program, circuits, gates
+
+from .plan_emulator import _apply_table
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-6
+
+
+def upload(wf, prec="fp64"):
+    n = int(np.log2(len(wf)))
+    s = CudaPureState(n, prec)
+    s.set_state_elements(wf)
+    return s
+
+
+def tol(prec):
+    return TOL64 if prec == "fp64" else TOL32
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_upload_download_roundtrip(gpu, prec):
+    for n in (1, 2, 5, 13, 17):
+        wf = circuits.random_state(n, seed=n)
+        s = upload(wf, prec)
+        got = s.state_elements()
+        if prec == "fp64":
+            np.testing.assert_array_equal(got, wf)
+        else:
+            np.testing.assert_array_equal(got, wf.astype(np.complex64).astype(np.complex128))
+        s.set_to_zero_state()
+        z = s.state_elements()
+        assert z[0] == 1 and np.count_nonzero(z) == 1
+        s.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_dense_all_tuples_small(gpu, oracle, prec):
+    """Every ordered qubit tuple of width 1..3 on a 6-qubit state, random
+    unitaries (the AVX-kernel-vs-Lisp style of tests/qvm-avx-intrinsics.lisp)."""
+    n = 6
+    rng = np.random.default_rng(1)
+    for k in (1, 2, 3):
+        for qs in itertools.permutations(range(n), k):
+            m = gates.haar_unitary(rng, 1 << k)
+            wf = circuits.random_state(n, seed=int(rng.integers(1 << 30)))
+            s = upload(wf, prec)
+            s.apply_matrix(m, list(qs))
+            want = oracle.apply_matrix_operator(wf.copy(), m, list(qs))
+            assert np.max(np.abs(s.state_elements() - want)) < tol(prec), (k, qs)
+            s.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+def test_dense_wide_and_real(gpu, oracle, prec, k):
+    n = 16
+    rng = np.random.default_rng(k)
+    for trial in range(6):
+        qs = [int(x) for x in rng.choice(n, k, replace=False)]
+        if trial % 2:
+            m = np.real(gates.haar_unitary(rng, 1 << k)) + 0j  # real-matrix kernel
+        else:
+            m = gates.haar_unitary(rng, 1 << k)
+        wf = circuits.random_state(n, seed=trial)
+        s = upload(wf, prec)
+        s.apply_matrix(m, qs)
+        want = oracle.apply_matrix_operator(wf.copy(), m, qs)
+        scale = max(1.0, np.max(np.abs(m)) * 4)
+        assert np.max(np.abs(s.state_elements() - want)) < tol(prec) * scale
+        s.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_permutation_and_diagonal(gpu, oracle, prec):
+    n = 12
+    rng = np.random.default_rng(3)
+    for trial in range(30):
+        k = int(rng.integers(1, 6))
+        qs = [int(x) for x in rng.choice(n, k, replace=False)]
+        wf = circuits.random_state(n, seed=trial)
+        s = upload(wf, prec)
+        perm = rng.permutation(1 << k)
+        s.apply_permutation(perm, qs)
+        want = oracle.apply_permutation(wf.copy(), perm, qs)
+        got = s.state_elements()
+        if prec == "fp64":
+            np.testing.assert_array_equal(got, want)  # pure data movement: bit-exact
+        else:
+            assert np.max(np.abs(got - want)) < TOL32
+        kd = int(rng.integers(1, 11))
+        qd = [int(x) for x in rng.choice(n, kd, replace=False)]
+        d = np.exp(1j * rng.uniform(0, 2 * np.pi, 1 << kd))
+        s.apply_diagonal(d, qd)
+        _apply_table(want, qd, d)
+        assert np.max(np.abs(s.state_elements() - want)) < tol(prec)
+        s.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_standard_gates(gpu, oracle, prec):
+    """Every standard gate through apply_dense (which routes permutation and
+    diagonal matrices to their kernels)."""
+    n = 7
+    rng = np.random.default_rng(4)
+    wf = circuits.random_state(n, seed=4)
+    s = upload(wf, prec)
+    want = wf.copy()
+    for name, (npar, _) in gates.STANDARD_GATES.items():
+        m = gates.gate_matrix(name, *rng.uniform(-3, 3, npar))
+        k = int(np.log2(m.shape[0]))
+        qs = [int(x) for x in rng.choice(n, k, replace=False)]
+        s.apply_matrix(m, qs)
+        oracle.apply_matrix_operator(want, m, qs)
+    assert np.max(np.abs(s.state_elements() - want)) < tol(prec) * 10
+    s.free()
+
+
+def _run_program(gs, n, prec, fused, init=None, fw=2, tile=0):
+    p = Program()
+    p.add_gates(gs)
+    if fused:
+        p.plan(n, prec, fused=True, fusion_width=fw, tile_qubits=tile)
+    s = CudaPureState(n, prec)
+    if init is not None:
+        s.set_state_elements(init)
+    p.run(s, fused=fused)
+    return s
+
+
+def _oracle(oracle, gs, n, init=None):
+    wf = oracle.zero_state(n) if init is None else init.copy()
+    for m, qs in gs:
+        oracle.apply_matrix_operator(wf, m, qs)
+    return wf
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("fused", [False, True])
+def test_layer_circuit_20q(gpu, oracle, prec, fused):
+    """Random RX/RZ + CNOT layer circuit at 20 qubits."""
+    n = 20
+    gs = circuits.random_layers(n, layers=10, seed=1)
+    want = _oracle(oracle, gs, n)
+    s = _run_program(gs, n, prec, fused)
+    got = s.state_elements()
+    assert np.max(np.abs(got - want)) < tol(prec)
+    if prec == "fp32":
+        f = abs(np.vdot(want, got)) ** 2
+        assert f >= 1 - 1e-6
+    s.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("fused", [False, True])
+def test_qft_on_random_state(gpu, oracle, prec, fused):
+    n = 16
+    gs = circuits.qft(n)
+    init = circuits.random_state(n, seed=2)
+    want = _oracle(oracle, gs, n, init)
+    s = _run_program(gs, n, prec, fused, init=init)
+    assert np.max(np.abs(s.state_elements() - want)) < tol(prec)
+    s.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("fw,tile", [(1, 0), (2, 0), (2, 10), (3, 12), (4, 11), (5, 13)])
+def test_random_su_fused(gpu, oracle, prec, fw, tile):
+    n = 18
+    gs = circuits.random_su_circuit(n, depth=6, seed=fw + tile)
+    want = _oracle(oracle, gs, n)
+    s = _run_program(gs, n, prec, True, fw=fw, tile=tile)
+    got = s.state_elements()
+    assert np.max(np.abs(got - want)) < tol(prec) * 2
+    s.free()
+
+
+def test_small_states_all_paths(gpu, oracle):
+    """States smaller than a tile row (n = 1..5) in every mode."""
+    for n in range(1, 6):
+        gs = circuits.random_su_circuit(n, depth=3, seed=n) if n > 1 else [
+            (gates.gate_matrix("H"), [0]), (gates.gate_matrix("RZ", 0.3), [0])]
+        want = _oracle(oracle, gs, n)
+        for prec in ("fp64", "fp32"):
+            for fused in (False, True):
+                s = _run_program(gs, n, prec, fused)
+                assert np.max(np.abs(s.state_elements() - want)) < tol(prec), (n, prec, fused)
+                s.free()
+
+
+def test_determinism_fp64(gpu):
+    n = 20
+    gs = circuits.random_su_circuit(n, depth=5, seed=8)
+    a = _run_program(gs, n, "fp64", True).state_elements()
+    b = _run_program(gs, n, "fp64", True).state_elements()
+    np.testing.assert_array_equal(a, b)
+
+
+def test_fp32_fidelity_26q(gpu):
+    """Fused FP32 vs plain FP64 on the device at 26 qubits, depth 20."""
+    n = 26
+    gs = circuits.random_su_circuit(n, depth=20, seed=3)
+    s64 = _run_program(gs, n, "fp64", False)
+    s32 = _run_program(gs, n, "fp32", True)
+    f, err = s64.fidelity(s32)
+    assert f >= 1 - 1e-6
+    assert err < 1e-5
+    assert abs(s32.norm() - 1) < 1e-5
+    s64.free()
+    s32.free()

@@ -1,0 +1,224 @@
+"""GPU parity: probabilities, measurement, collapse and sampling against the
+CPU oracle and the reference's known answers.
+
+Sampled indices must be identical for identical draws, except for draws
+within 1e-12 of a CDF boundary (the sums are taken in a different order).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from qvm_gb300 import CudaPureState, PureStateQVM, circuits
+
+from .test_oracle_kat import KATS, kat_vector, lisp_accumulated_draws
+
+pytestmark = pytest.mark.gpu
+
+
+def upload(wf, prec="fp64"):
+    n = max(1, int(np.log2(len(wf))))
+    s = CudaPureState(n, prec)
+    s.set_state_elements(wf)
+    return s
+
+
+def near_boundary(cdf, draws, eps=1e-12):
+    return np.array([np.min(np.abs(cdf - d)) < eps for d in draws])
+
+
+def test_sampler_kats(gpu):
+    """tests/measurement-tests.lisp:184-211 through the device sampler."""
+    for c in KATS["sample_wavefunction"]["cases"]:
+        v = kat_vector(c["probs_single"])
+        draws = c["draws"]
+        if isinstance(draws, str):
+            draws = lisp_accumulated_draws(0.1, len(c["expected"]))
+        s = upload(v)
+        got = [int(x) for x in s.sample(draws, rule="bisect")]
+        assert got == c["expected"], (c, got)
+        s.free()
+
+
+def test_measure_all_basis_states(gpu):
+    """tests/measurement-tests.lisp:213-237"""
+    n = KATS["measure_all_basis"]["n"]
+    for i in range(1 << n):
+        prog = "\n".join(("X %d" % q) if (i >> q) & 1 else ("I %d" % q) for q in range(n))
+        for prec in ("fp64", "fp32"):
+            qvm = PureStateQVM(n, precision=prec, seed=1)
+            qvm.load_program(prog).run()
+            _, bits = qvm.measure_all()
+            assert bits == [(i >> q) & 1 for q in range(n)]
+            amps = qvm.amplitudes
+            assert amps[i] == 1 and np.count_nonzero(amps) == 1
+            qvm.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_excited_ground_probability(gpu, oracle, prec):
+    for n in (1, 3, 12, 21):
+        wf = circuits.random_state(n, seed=n)
+        s = upload(wf, prec)
+        ref = wf if prec == "fp64" else wf.astype(np.complex64).astype(np.complex128)
+        for q in sorted({0, n // 2, n - 1}):
+            p1 = s.excited_probability(q)
+            p0 = s.ground_probability(q)
+            assert abs(p1 - oracle.excited_probability(ref, q)) < 1e-13
+            assert abs(p0 - oracle.ground_probability(ref, q)) < 1e-13
+        assert abs(s.norm() - oracle.norm(ref)) < 1e-13
+        s.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("compiled", [False, True])
+def test_measure_matches_oracle(gpu, oracle, prec, compiled):
+    n = 14
+    rng = np.random.default_rng(5)
+    wf = circuits.random_state(n, seed=5)
+    ref = wf if prec == "fp64" else wf.astype(np.complex64).astype(np.complex128)
+    s = upload(wf, prec)
+    want = ref.copy()
+    for q in rng.permutation(n)[:6]:
+        draw = rng.random()
+        bit, used, prob = s.measure(int(q), draw, compiled=compiled)
+        if compiled:
+            wbit, wprob = oracle.measure_compiled(want, int(q), draw)
+            wused = True
+        else:
+            wbit, wused, wprob = oracle.measure(want, int(q), draw)
+        assert abs(prob - wprob) < 1e-12
+        if abs(draw - wprob) > 1e-12:
+            assert bit == wbit and used == wused
+        tol = 1e-12 if prec == "fp64" else 2e-6
+        assert np.max(np.abs(s.state_elements() - want)) < tol
+    s.free()
+
+
+def test_measure_skips_draw_when_p1_zero(gpu):
+    s = CudaPureState(3)
+    bit, used, p1 = s.measure(2, 0.0)
+    assert (bit, used, p1) == (0, False, 0.0)
+    s.free()
+
+
+def test_force_measurement(gpu, oracle):
+    n = 10
+    wf = circuits.random_state(n, seed=6)
+    s = upload(wf)
+    p1 = s.excited_probability(4)
+    s.force_measurement(1, 4, p1)
+    want = oracle.force_measurement(wf.copy(), 1, 4, oracle.excited_probability(wf, 4))
+    assert np.max(np.abs(s.state_elements() - want)) < 1e-12
+    z = CudaPureState(2)
+    from qvm_gb300 import QVMGError
+    with pytest.raises(QVMGError, match="cannot force"):
+        z.force_measurement(1, 0, 0.0)
+    s.free()
+    z.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("rule", ["bisect", "cdf"])
+def test_sample_matches_oracle(gpu, oracle, prec, rule):
+    rng = np.random.default_rng(7)
+    for n in (1, 4, 12, 13, 20):
+        wf = circuits.random_state(n, seed=n + 100)
+        ref = wf if prec == "fp64" else wf.astype(np.complex64).astype(np.complex128)
+        s = upload(wf, prec)
+        draws = rng.random(512)
+        got = s.sample(draws, rule=rule)
+        if rule == "bisect":
+            want = np.array([oracle.sample_bisect(ref, p) for p in draws])
+        else:
+            want = oracle.sample_multiple(ref, draws)
+        cdf = np.cumsum(np.abs(ref) ** 2)
+        ok = (got == want) | near_boundary(cdf, draws)
+        assert ok.all(), (n, np.nonzero(~ok))
+        s.free()
+
+
+def test_sample_edges(gpu, oracle):
+    """Zero-probability prefix, p = 0, p = 1 and p beyond the total."""
+    v = np.zeros(1 << 13, dtype=np.complex128)
+    v[5000] = np.sqrt(0.25)
+    v[8191] = np.sqrt(0.75)
+    s = upload(v)
+    draws = [0.0, 0.1, 0.25, 0.2500001, 0.9999, 1.0]
+    for rule in ("bisect", "cdf"):
+        got = list(s.sample(draws, rule=rule))
+        if rule == "bisect":
+            want = [oracle.sample_bisect(v, p) for p in draws]
+        else:
+            want = list(oracle.sample_multiple(v, draws))
+        assert got == want, (rule, got, want)
+    s.free()
+
+
+def test_measure_all_matches_oracle(gpu, oracle):
+    rng = np.random.default_rng(8)
+    for n in (2, 11, 16):
+        wf = circuits.random_state(n, seed=n)
+        for _ in range(4):
+            draw = rng.random()
+            s = upload(wf)
+            idx = s.measure_all(draw)
+            want_wf = wf.copy()
+            widx = oracle.measure_all(want_wf, draw)
+            assert idx == widx
+            np.testing.assert_array_equal(s.state_elements(), want_wf)
+            s.free()
+
+
+def test_probabilities_and_inner(gpu, oracle):
+    n = 15
+    a = circuits.random_state(n, seed=1)
+    b = circuits.random_state(n, seed=2)
+    sa, sb = upload(a), upload(b)
+    np.testing.assert_allclose(sa.probabilities(), np.abs(a) ** 2, rtol=0, atol=1e-16)
+    z = sa.inner(sb)
+    w = oracle.inner(a, b)
+    assert abs(z - w) < 1e-13
+    f, err = sa.fidelity(sb)
+    assert abs(f - abs(w) ** 2) < 1e-13
+    assert abs(err - np.max(np.abs(a - b))) < 1e-13
+    sb32 = CudaPureState(n, "fp32")
+    sb32.copy_from(sb)
+    f32, _ = sb.fidelity(sb32)
+    assert f32 >= 1 - 1e-12
+    sa.free()
+    sb.free()
+    sb32.free()
+
+
+def test_normalize(gpu):
+    n = 12
+    wf = circuits.random_state(n, seed=3) * 3.0
+    s = upload(wf)
+    s.normalize()
+    assert abs(s.norm() - 1) < 1e-14
+    np.testing.assert_allclose(s.state_elements(), wf / np.linalg.norm(wf), atol=1e-15)
+    s.free()
+
+
+def test_sample_bell_distribution_20q(gpu):
+    """Config-1 circuit at 20 qubits, 1000 shots from the same uniform draws
+    on the device and in the oracle: identical bitstrings."""
+    from oracle import oracle as O
+    n = 20
+    gs = circuits.random_layers(n, layers=10, seed=1)
+    wf = O.zero_state(n)
+    for m, qs in gs:
+        O.apply_matrix_operator(wf, m, qs)
+    from qvm_gb300 import Program
+    p = Program()
+    p.add_gates(gs)
+    s = CudaPureState(n)
+    p.run(s, fused=False)
+    draws = np.random.default_rng(20).random(1000)
+    got = s.sample(draws, rule="bisect")
+    want = np.array([O.sample_bisect(wf, d) for d in draws])
+    cdf = np.cumsum(np.abs(wf) ** 2)
+    assert ((got == want) | near_boundary(cdf, draws)).all()
+    s.free()
