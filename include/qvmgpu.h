@@ -149,7 +149,8 @@ int qvmg_norm(qvmg_state s, double *norm);
 int qvmg_normalize(qvmg_state s);
 /* inner product sum conj(a_i) b_i (app/src/api/expectation.lisp:80-84). */
 int qvmg_inner(qvmg_state a, qvmg_state b, double *re, double *im);
-/* |<a|b>|^2 and max_i |a_i - b_i| (precision report of the fused form). */
+/* |<a|b>|^2 / (<a|a><b|b>) and max_i |a_i - b_i| (precision report of the
+ * fused form; the FP32 form is compared as a normalised state). */
 int qvmg_fidelity(qvmg_state a, qvmg_state b, double *fidelity, double *max_abs_err);
 
 /* ---- programs: transition loop over gate applications ------------------- */
@@ -188,6 +189,31 @@ int qvmg_program_run_profiled(qvmg_state s, qvmg_program p, int mode, float *pas
 /* The cudaStream_t (as void*) the state's work is ordered on, so a caller
  * can order or time its own work against it. */
 int qvmg_state_stream(qvmg_state s, void **stream);
+
+/* ---- batched QAOA MaxCut instances -------------------------------------- */
+/* Many uneven QAOA circuits (examples/qaoa.lisp:7-206: H on all qubits, then
+ * p layers of ZZ(gamma) on every graph edge and RX(2 beta) on every qubit)
+ * held as complex FP32 states and run in one persistent launch with a device
+ * work queue, captured once as a CUDA graph.  The multishot sampling of
+ * each result follows sample-wavefunction-multiple-times
+ * (src/measurement.lisp:246-288) with caller-supplied draws.
+ * edges: flat (u, v) pairs of all instances in order; nedges[i] per
+ * instance; qubit counts 2..26; p <= 16; <= 64 edges per instance. */
+typedef struct qvmg_qaoa_s *qvmg_qaoa_batch;
+int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, const int *edges,
+                           int p, const double *gammas, const double *betas,
+                           qvmg_qaoa_batch *out);
+/* Replace the angles (ninst x p each) for the next run. */
+int qvmg_qaoa_batch_set_angles(qvmg_qaoa_batch b, const double *gammas, const double *betas);
+/* Run every instance: expectations[i] = <H_C> (FP64 sum of |a_x|^2 cut(x));
+ * shots[i*nshots + t] = smallest x with C(x) >= draws[i*nshots + t]. */
+int qvmg_qaoa_batch_run(qvmg_qaoa_batch b, const double *draws, int nshots,
+                        double *expectations, uint32_t *shots);
+/* Final state of one instance as complex128 (2^n values). */
+int qvmg_qaoa_batch_state(qvmg_qaoa_batch b, int instance, double *amps);
+/* Device bytes the batch holds. */
+uint64_t qvmg_qaoa_batch_bytes(qvmg_qaoa_batch b);
+int qvmg_qaoa_batch_free(qvmg_qaoa_batch b);
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,12 @@ SIGNATURES = {
     "qvmg_program_run": (_i, [_vp, _vp, _i]),
     "qvmg_program_run_profiled": (_i, [_vp, _vp, _i, ctypes.POINTER(ctypes.c_float), _ip, _i, _ip]),
     "qvmg_state_stream": (_i, [_vp, _vpp]),
+    "qvmg_qaoa_batch_create": (_i, [_i, _ip, _ip, _ip, _i, _dp, _dp, _vpp]),
+    "qvmg_qaoa_batch_set_angles": (_i, [_vp, _dp, _dp]),
+    "qvmg_qaoa_batch_run": (_i, [_vp, _dp, _i, _dp, ctypes.POINTER(ctypes.c_uint32)]),
+    "qvmg_qaoa_batch_state": (_i, [_vp, _i, _dp]),
+    "qvmg_qaoa_batch_bytes": (_u64, [_vp]),
+    "qvmg_qaoa_batch_free": (_i, [_vp]),
 }
 
 STATUS = {

@@ -18,7 +18,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libqvmgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["state.cu", "gates.cu", "measure.cu", "tile.cu", "program.cu", "plan.cpp"]
+SOURCES = ["state.cu", "gates.cu", "measure.cu", "tile.cu", "program.cu", "plan.cpp",
+           "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
               "-Wall", "--expt-relaxed-constexpr", "-I", INCLUDE]

@@ -1,0 +1,517 @@
+// batch.cu -- batched QAOA MaxCut instances in one persistent launch.
+//
+// The reference runs one QVM per request and re-runs the program per trial
+// (app/src/api/multishot.lisp:87-101; examples/qaoa.lisp:118-183 samples
+// each QAOA wavefunction with sample-wavefunction-multiple-times).  Here a
+// batch of uneven instances (different qubit counts, graphs and angles) runs
+// in one persistent kernel: each CTA takes the next instance from a device
+// work queue (an atomic counter, instances sorted largest first) and runs
+// the whole circuit for it:
+//   H on all qubits                 -> amplitudes start at 2^(-n/2)
+//   per layer l: ZZ(gamma_l) on every edge, i.e. the diagonal
+//                exp(-i gamma_l (m - 2 cut(x)) / 2), then RX(2 beta_l) on
+//                every qubit
+//   <H_C> = sum_x |a_x|^2 cut(x)   (FP64 accumulation)
+//   shots: a two-level CDF (128-amplitude sub-block sums, FP64 prefix)
+//          searched per draw by one warp, smallest x with C(x) >= draw.
+// States of <= 13 qubits live in shared memory for the whole circuit; larger
+// ones stay in HBM and are swept in two tile passes per layer (low 13 qubits
+// contiguous; then the high qubits with a 2^(26-n)-amplitude row).  Amplitudes
+// are complex FP32; the phase table and RX coefficients are computed in FP64.
+// All spin-free: the queue is a plain atomicAdd, no CTA waits on another.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "cplx.h"
+#include "internal.h"
+
+namespace qvmg {
+
+constexpr int kQaoaTileBits = 13;
+constexpr int kQaoaThreads = 512;
+constexpr int kQaoaMaxEdges = 64;
+constexpr int kQaoaMaxLayers = 16;
+constexpr int kQaoaSubBits = 7;  // 128-amplitude CDF sub-blocks
+
+struct QaoaInst {
+  unsigned long long state_off;  // float2 offset of the state
+  unsigned long long sub_off;    // double offset of the CDF sub-block sums
+  int n;
+  int nedges;
+  int edge_off;   // into edges (pairs)
+  int param_off;  // into gammas / betas (p values)
+  int id;         // caller's instance index
+  int pad;
+};
+
+struct QaoaArgs {
+  int ninst;
+  int p;
+  int nshots;
+  int pad;
+  const QaoaInst *inst;
+  const unsigned char *edges;  // pairs (u, v)
+  const double *gammas;
+  const double *betas;
+  float2 *states;
+  double *subs;
+  const double *draws;        // ninst * nshots, indexed by instance id
+  double *expect;             // ninst
+  unsigned int *shots;        // ninst * nshots
+  unsigned int *counter;      // work queue head
+};
+
+__device__ __forceinline__ int cut_value(unsigned long long x, const unsigned char *e, int m) {
+  int c = 0;
+  for (int i = 0; i < m; ++i) c += (int)(((x >> e[2 * i]) ^ (x >> e[2 * i + 1])) & 1ull);
+  return c;
+}
+
+__device__ __forceinline__ float2 rx_apply_lo(float2 a, float2 b, float c, float s) {
+  // row 0 of [[c, -is], [-is, c]] * (a, b)
+  return make_float2(c * a.x + s * b.y, c * a.y - s * b.x);
+}
+
+// RX(2 beta) on local bit `bit` of a shared-memory tile of 2^tb amplitudes.
+__device__ __forceinline__ void tile_rx(float2 *tile, int tb, int bit, float c, float s) {
+  const unsigned npairs = 1u << (tb - 1);
+  for (unsigned g = threadIdx.x; g < npairs; g += blockDim.x) {
+    unsigned lo = g & ((1u << bit) - 1u);
+    unsigned i0 = ((g >> bit) << (bit + 1)) | lo;
+    unsigned i1 = i0 | (1u << bit);
+    float2 a = tile[i0], b = tile[i1];
+    tile[i0] = rx_apply_lo(a, b, c, s);
+    tile[i1] = rx_apply_lo(b, a, c, s);
+  }
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double prob_d(float2 v) {
+  return (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+}
+
+__global__ void __launch_bounds__(kQaoaThreads) k_qaoa_batch(const __grid_constant__ QaoaArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *tile = reinterpret_cast<float2 *>(smem);                     // 2^13
+  float2 *phase = tile + (1u << kQaoaTileBits);                         // kQaoaMaxEdges+1
+  unsigned char *edges = reinterpret_cast<unsigned char *>(phase + kQaoaMaxEdges + 1);
+  __shared__ double red[kQaoaThreads / 32];
+  __shared__ int s_inst;
+  __shared__ float s_c, s_s;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_inst = (int)atomicAdd(A.counter, 1u);
+    __syncthreads();
+    const int k = s_inst;
+    if (k >= A.ninst) break;
+    const QaoaInst I = A.inst[k];
+    const int n = I.n, m = I.nedges;
+    float2 *psi = A.states + I.state_off;
+    for (int i = threadIdx.x; i < 2 * m; i += blockDim.x) edges[i] = A.edges[2 * I.edge_off + i];
+    const unsigned long long len = 1ull << n;
+    const float amp0 = (float)(1.0 / sqrt((double)len));
+    const bool resident = n <= kQaoaTileBits;
+    if (resident) {
+      for (unsigned x = threadIdx.x; x < len; x += blockDim.x) tile[x] = make_float2(amp0, 0.f);
+    } else {
+      for (unsigned long long x = threadIdx.x; x < len; x += blockDim.x)
+        psi[x] = make_float2(amp0, 0.f);
+    }
+    for (int l = 0; l < A.p; ++l) {
+      const double g = A.gammas[I.param_off + l], b = A.betas[I.param_off + l];
+      __syncthreads();
+      for (int c = threadIdx.x; c <= m; c += blockDim.x) {
+        double sn, cs;
+        sincos(-g * (double)(m - 2 * c) * 0.5, &sn, &cs);
+        phase[c] = make_float2((float)cs, (float)sn);
+      }
+      if (threadIdx.x == 0) {
+        double sn, cs;
+        sincos(b, &sn, &cs);
+        s_c = (float)cs;
+        s_s = (float)sn;
+      }
+      __syncthreads();
+      const float c = s_c, s = s_s;
+      if (resident) {
+        for (unsigned x = threadIdx.x; x < len; x += blockDim.x)
+          tile[x] = cmul(tile[x], phase[cut_value(x, edges, m)]);
+        __syncthreads();
+        for (int q = 0; q < n; ++q) {
+          tile_rx(tile, n, q, c, s);
+          __syncthreads();
+        }
+      } else {
+        const int tb = kQaoaTileBits;
+        const unsigned long long ntiles = len >> tb;
+        // pass A: contiguous tiles, phase + RX on qubits 0..12
+        for (unsigned long long tcount = 0; tcount < ntiles; ++tcount) {
+          const unsigned long long base = tcount << tb;
+          __syncthreads();
+          for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
+            reinterpret_cast<float4 *>(tile)[j] = reinterpret_cast<const float4 *>(psi + base)[j];
+          __syncthreads();
+          for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
+            tile[j] = cmul(tile[j], phase[cut_value(base + j, edges, m)]);
+          __syncthreads();
+          for (int q = 0; q < tb; ++q) {
+            tile_rx(tile, tb, q, c, s);
+            __syncthreads();
+          }
+          for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
+            reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
+        }
+        // pass B: rows of 2^Lb amplitudes, the high qubits 13..n-1 in the tile
+        const int hb = n - tb, Lb = tb - hb;  // n <= 26 keeps Lb >= 0
+        for (unsigned long long cidx = 0; cidx < ntiles; ++cidx) {
+          __syncthreads();
+          for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x) {
+            unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
+            tile[j] = psi[(h << tb) | (cidx << Lb) | lo];
+          }
+          __syncthreads();
+          for (int q = 0; q < hb; ++q) {
+            tile_rx(tile, tb, Lb + q, c, s);
+            __syncthreads();
+          }
+          for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x) {
+            unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
+            psi[(h << tb) | (cidx << Lb) | lo] = tile[j];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (resident) {
+      for (unsigned x = threadIdx.x; x < len; x += blockDim.x) psi[x] = tile[x];
+      __syncthreads();
+    }
+    // expectation and 128-amplitude sub-block sums (one warp per sub-block)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int sbits = n < kQaoaSubBits ? n : kQaoaSubBits;
+    const unsigned long long nsub = len >> sbits;
+    double *sub = A.subs + I.sub_off;
+    double ex = 0.0;
+    for (unsigned long long sb = warp; sb < nsub; sb += nwarps) {
+      float hi = 0.f, lo = 0.f, exf = 0.f;
+      for (unsigned j = lane; j < (1u << sbits); j += 32) {
+        unsigned long long x = (sb << sbits) + j;
+        float2 v = psi[x];
+        df_add_prob(hi, lo, v);  // exact squares for the CDF
+        exf = fmaf(fmaf(v.x, v.x, v.y * v.y), (float)cut_value(x, edges, m), exf);
+      }
+      double acc = warp_sum_d((double)hi + (double)lo);
+      ex += (double)exf;
+      if (lane == 0) sub[sb] = acc;
+    }
+    ex = warp_sum_d(ex);
+    if (lane == 0) red[warp] = ex;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double e = 0.0;
+      for (int w = 0; w < nwarps; ++w) e += red[w];
+      A.expect[I.id] = e;
+    }
+    // inclusive prefix over the sub-block sums: per-thread chunks, then a
+    // scan of the chunk totals in shared memory (the tile is free now)
+    {
+      double *tot = reinterpret_cast<double *>(tile);
+      const unsigned long long per = (nsub + blockDim.x - 1) / blockDim.x;
+      const unsigned long long a0 = threadIdx.x * per;
+      const unsigned long long a1 = min(nsub, a0 + per);
+      double s = 0.0;
+      for (unsigned long long i = a0; i < a1; ++i) s += sub[i];
+      tot[threadIdx.x] = s;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (unsigned w = 0; w < blockDim.x; ++w) {
+          double v = tot[w];
+          tot[w] = r;
+          r += v;
+        }
+      }
+      __syncthreads();
+      double r = tot[threadIdx.x];
+      for (unsigned long long i = a0; i < a1; ++i) {
+        r += sub[i];
+        sub[i] = r;
+      }
+    }
+    __syncthreads();
+    // shots: smallest x with C(x) >= draw (src/measurement.lisp:246-288), len-1 if none
+    for (int t = warp; t < A.nshots; t += nwarps) {
+      const double p = A.draws[(unsigned long long)I.id * A.nshots + t];
+      unsigned long long lo = 0, hi = nsub;
+      while (lo < hi) {
+        unsigned long long mid = (lo + hi) >> 1;
+        if (sub[mid] >= p) hi = mid; else lo = mid + 1;
+      }
+      unsigned int res = (unsigned int)(len - 1);
+      if (lo < nsub) {
+        double run = lo ? sub[lo - 1] : 0.0;
+        res = (unsigned int)(((lo + 1) << sbits) - 1);
+        for (unsigned c0 = 0; c0 < (1u << sbits); c0 += 32) {
+          const bool valid = c0 + lane < (1u << sbits);
+          double pr = valid ? prob_d(psi[(lo << sbits) + c0 + lane]) : 0.0;
+          double sc = pr;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            double y = __shfl_up_sync(0xffffffffu, sc, o);
+            if (lane >= o) sc += y;
+          }
+          unsigned msk = __ballot_sync(0xffffffffu, valid && run + sc >= p);
+          if (msk) {
+            res = (unsigned int)((lo << sbits) + c0 + (__ffs(msk) - 1));
+            break;
+          }
+          run += __shfl_sync(0xffffffffu, sc, 31);
+        }
+      }
+      if (lane == 0) A.shots[(unsigned long long)I.id * A.nshots + t] = res;
+    }
+  }
+}
+
+}  // namespace qvmg
+
+struct qvmg_qaoa_s {
+  int ninst = 0, p = 0;
+  std::vector<int> n;                // per caller instance
+  std::vector<unsigned long long> state_off;
+  qvmg::QaoaArgs args{};
+  void *dbuf = nullptr;              // instances, edges, params
+  float2 *states = nullptr;
+  double *subs = nullptr;
+  double *draws = nullptr;
+  double *expect = nullptr;
+  unsigned int *shots = nullptr;
+  unsigned int *counter = nullptr;
+  int nshots_cap = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_shots = -1;
+  uint64_t bytes = 0;
+};
+
+using namespace qvmg;
+
+static void qaoa_release(qvmg_qaoa_batch b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->dbuf);
+  cudaFree(b->states);
+  cudaFree(b->subs);
+  cudaFree(b->draws);
+  cudaFree(b->expect);
+  cudaFree(b->shots);
+  cudaFree(b->counter);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+extern "C" {
+
+int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, const int *edges,
+                           int p, const double *gammas, const double *betas,
+                           qvmg_qaoa_batch *out) {
+  if (!out) return fail(QVMG_E_INVALID, "null output handle");
+  *out = nullptr;
+  if (ninst < 1 || !nqubits || !nedges || !edges || !gammas || !betas)
+    return fail(QVMG_E_INVALID, "empty batch or null array");
+  if (p < 1 || p > kQaoaMaxLayers) return fail(QVMG_E_INVALID, "QAOA depth must be 1..16");
+  std::vector<QaoaInst> inst(ninst);
+  std::vector<unsigned char> e8;
+  unsigned long long soff = 0, uoff = 0;
+  int eoff = 0;
+  for (int i = 0; i < ninst; ++i) {
+    int n = nqubits[i];
+    if (n < 2 || n > 26) return fail(QVMG_E_INVALID, "instance qubit count must be 2..26");
+    if (nedges[i] < 0 || nedges[i] > kQaoaMaxEdges)
+      return fail(QVMG_E_INVALID, "instance edge count must be 0..64");
+    inst[i].n = n;
+    inst[i].nedges = nedges[i];
+    inst[i].edge_off = eoff;
+    inst[i].param_off = i * p;
+    inst[i].id = i;
+    for (int j = 0; j < nedges[i]; ++j) {
+      int u = edges[2 * (eoff + j)], v = edges[2 * (eoff + j) + 1];
+      if (u < 0 || v < 0 || u >= n || v >= n || u == v)
+        return fail(QVMG_E_INVALID, "edge (" + std::to_string(u) + "," + std::to_string(v) +
+                                        ") invalid for instance " + std::to_string(i));
+      e8.push_back((unsigned char)u);
+      e8.push_back((unsigned char)v);
+    }
+    eoff += nedges[i];
+  }
+  // largest instances first: the queue hands them out before the small ones
+  std::vector<int> order(ninst);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return inst[a].n > inst[b].n; });
+  std::vector<QaoaInst> sorted(ninst);
+  qvmg_qaoa_batch b = new qvmg_qaoa_s();
+  b->ninst = ninst;
+  b->p = p;
+  b->n.assign(nqubits, nqubits + ninst);
+  b->state_off.assign(ninst, 0);
+  for (int r = 0; r < ninst; ++r) {
+    QaoaInst q = inst[order[r]];
+    q.state_off = soff;
+    q.sub_off = uoff;
+    b->state_off[q.id] = soff;
+    soff += 1ull << q.n;
+    int sb = q.n < kQaoaSubBits ? q.n : kQaoaSubBits;
+    uoff += 1ull << (q.n - sb);
+    sorted[r] = q;
+  }
+  size_t ib = sizeof(QaoaInst) * ninst, eb = (e8.size() + 15) & ~(size_t)15,
+         pb = sizeof(double) * (size_t)ninst * p;
+  std::vector<unsigned char> host(ib + eb + 2 * pb, 0);
+  std::memcpy(host.data(), sorted.data(), ib);
+  if (!e8.empty()) std::memcpy(host.data() + ib, e8.data(), e8.size());
+  std::memcpy(host.data() + ib + eb, gammas, pb);
+  std::memcpy(host.data() + ib + eb + pb, betas, pb);
+  cudaError_t e;
+#define QCHK(call, what)                         \
+  if ((e = (call)) != cudaSuccess) {             \
+    int rc = cuda_fail(e, what);                 \
+    qaoa_release(b);                             \
+    return rc;                                   \
+  }
+  QCHK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  QCHK(cudaMalloc(&b->dbuf, host.size()), "cudaMalloc(batch tables)");
+  QCHK(cudaMemcpy(b->dbuf, host.data(), host.size(), cudaMemcpyHostToDevice), "cudaMemcpy");
+  QCHK(cudaMalloc(&b->states, soff * sizeof(float2)), "cudaMalloc(batch states)");
+  QCHK(cudaMalloc(&b->subs, uoff * sizeof(double)), "cudaMalloc(batch CDF)");
+  QCHK(cudaMalloc(&b->expect, ninst * sizeof(double)), "cudaMalloc(expectations)");
+  QCHK(cudaMalloc(&b->counter, sizeof(unsigned int)), "cudaMalloc(counter)");
+#undef QCHK
+  b->bytes = host.size() + soff * sizeof(float2) + uoff * sizeof(double) + ninst * 8;
+  QaoaArgs &A = b->args;
+  A.ninst = ninst;
+  A.p = p;
+  A.inst = (const QaoaInst *)b->dbuf;
+  A.edges = (const unsigned char *)b->dbuf + ib;
+  A.gammas = (const double *)((unsigned char *)b->dbuf + ib + eb);
+  A.betas = (const double *)((unsigned char *)b->dbuf + ib + eb + pb);
+  A.states = b->states;
+  A.subs = b->subs;
+  A.expect = b->expect;
+  A.counter = b->counter;
+  static bool attr = false;
+  if (!attr) {
+    int bytes = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges + 16;
+    e = cudaFuncSetAttribute(k_qaoa_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) {
+      qaoa_release(b);
+      return cuda_fail(e, "cudaFuncSetAttribute(k_qaoa_batch)");
+    }
+    attr = true;
+  }
+  *out = b;
+  return QVMG_OK;
+}
+
+int qvmg_qaoa_batch_set_angles(qvmg_qaoa_batch b, const double *gammas, const double *betas) {
+  if (!b || !gammas || !betas) return fail(QVMG_E_INVALID, "null batch or angles");
+  size_t pb = sizeof(double) * (size_t)b->ninst * b->p;
+  QVMG_CUDA(cudaMemcpyAsync((void *)b->args.gammas, gammas, pb, cudaMemcpyHostToDevice, b->stream));
+  QVMG_CUDA(cudaMemcpyAsync((void *)b->args.betas, betas, pb, cudaMemcpyHostToDevice, b->stream));
+  QVMG_CUDA(cudaStreamSynchronize(b->stream));
+  return QVMG_OK;
+}
+
+int qvmg_qaoa_batch_run(qvmg_qaoa_batch b, const double *draws, int nshots, double *expectations,
+                        uint32_t *shots) {
+  if (!b) return fail(QVMG_E_INVALID, "null batch");
+  if (nshots < 0 || (nshots > 0 && (!draws || !shots)))
+    return fail(QVMG_E_INVALID, "shots requested without draws or output");
+  if (nshots > b->nshots_cap) {
+    QVMG_CUDA(cudaStreamSynchronize(b->stream));
+    cudaFree(b->draws);
+    cudaFree(b->shots);
+    b->draws = nullptr;
+    b->shots = nullptr;
+    QVMG_CUDA(cudaMalloc(&b->draws, sizeof(double) * (size_t)b->ninst * nshots));
+    QVMG_CUDA(cudaMalloc(&b->shots, sizeof(unsigned int) * (size_t)b->ninst * nshots));
+    b->nshots_cap = nshots;
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
+  QaoaArgs &A = b->args;
+  A.nshots = nshots;
+  A.draws = b->draws;
+  A.shots = b->shots;
+  if (nshots > 0)
+    QVMG_CUDA(cudaMemcpyAsync(b->draws, draws, sizeof(double) * (size_t)b->ninst * nshots,
+                              cudaMemcpyHostToDevice, b->stream));
+  // The queue reset and the persistent kernel are one captured graph,
+  // replayed on every run with the same shot count.
+  if (!b->graph || b->graph_shots != nshots) {
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+    cudaGraph_t g;
+    QVMG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(b->counter, 0, sizeof(unsigned int), b->stream);
+    int smem = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges + 16;
+    int grid = std::min(b->ninst, sm_count() * 3);
+    k_qaoa_batch<<<grid, kQaoaThreads, smem, b->stream>>>(A);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (le != cudaSuccess) return cuda_fail(le, "k_qaoa_batch launch");
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
+    b->graph_shots = nshots;
+  }
+  QVMG_CUDA(cudaGraphLaunch(b->graph, b->stream));
+  if (expectations)
+    QVMG_CUDA(cudaMemcpyAsync(expectations, b->expect, sizeof(double) * b->ninst,
+                              cudaMemcpyDeviceToHost, b->stream));
+  if (nshots > 0)
+    QVMG_CUDA(cudaMemcpyAsync(shots, b->shots, sizeof(unsigned int) * (size_t)b->ninst * nshots,
+                              cudaMemcpyDeviceToHost, b->stream));
+  QVMG_CUDA(cudaStreamSynchronize(b->stream));
+  return QVMG_OK;
+}
+
+int qvmg_qaoa_batch_state(qvmg_qaoa_batch b, int instance, double *amps) {
+  if (!b || !amps) return fail(QVMG_E_INVALID, "null batch or buffer");
+  if (instance < 0 || instance >= b->ninst) return fail(QVMG_E_INVALID, "instance out of range");
+  uint64_t len = 1ull << b->n[instance];
+  std::vector<float2> tmp(len);
+  QVMG_CUDA(cudaMemcpyAsync(tmp.data(), b->states + b->state_off[instance], len * sizeof(float2),
+                            cudaMemcpyDeviceToHost, b->stream));
+  QVMG_CUDA(cudaStreamSynchronize(b->stream));
+  for (uint64_t i = 0; i < len; ++i) {
+    amps[2 * i] = tmp[i].x;
+    amps[2 * i + 1] = tmp[i].y;
+  }
+  return QVMG_OK;
+}
+
+uint64_t qvmg_qaoa_batch_bytes(qvmg_qaoa_batch b) { return b ? b->bytes : 0; }
+
+int qvmg_qaoa_batch_free(qvmg_qaoa_batch b) {
+  qaoa_release(b);
+  return QVMG_OK;
+}
+
+}  // extern "C"

@@ -57,4 +57,38 @@ __host__ __device__ __forceinline__ uint64_t inject0(uint64_t x, int q) {
   return ((x >> q) << (q + 1)) | lo;
 }
 
+// ---- FP64-accurate probabilities of FP32 amplitudes --------------------------
+__device__ __forceinline__ double amp_prob(double2 v) { return fma(v.x, v.x, v.y * v.y); }
+
+// Two-sum of a float into (hi, lo).
+__device__ __forceinline__ void df_add(float &hi, float &lo, float x) {
+  float s = hi + x;
+  float bp = s - hi;
+  float e = (hi - (s - bp)) + (x - bp);
+  hi = s;
+  lo += e;
+}
+
+// Add |v|^2 of an FP32 amplitude into (hi, lo) without rounding the
+// squares: x*x = p + e exactly with e = fma(x, x, -p).  The error terms of
+// the squares and of the two-sums are gathered in lo.
+__device__ __forceinline__ void df_add_prob(float &hi, float &lo, float2 v) {
+  float pr = v.x * v.x, er = fmaf(v.x, v.x, -pr);
+  float pi = v.y * v.y, ei = fmaf(v.y, v.y, -pi);
+  float s = pr + pi;
+  float bp = s - pr;
+  float es = (pr - (s - bp)) + (pi - bp);
+  df_add(hi, lo, s);
+  lo += (er + ei) + es;
+}
+
+// |v|^2 as a double for an FP32 amplitude: exact squares, rounded once.
+__device__ __forceinline__ double prob_f64(float2 v) {
+  float hi = 0.f, lo = 0.f;
+  df_add_prob(hi, lo, v);
+  return (double)hi + (double)lo;
+}
+__device__ __forceinline__ double prob_f64(double2 v) { return fma(v.x, v.x, v.y * v.y); }
+
+
 }  // namespace qvmg

@@ -32,6 +32,7 @@ struct MeasResult {
   double prob;      // p1 (interpreted) or p0 (compiled) or sum for norms
   double inv_norm;  // renormalisation factor of the kept half
   double aux;       // imaginary part / second reduction value
+  double na, nb;    // squared norms of the two states of an inner product
   int bit;          // measured bit
   int draw_used;    // whether the draw was consumed
   unsigned long long index;  // measure-all index

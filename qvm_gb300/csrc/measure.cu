@@ -33,38 +33,6 @@
 namespace qvmg {
 
 // ---- accumulation helpers ----------------------------------------------------
-__device__ __forceinline__ double amp_prob(double2 v) { return fma(v.x, v.x, v.y * v.y); }
-
-// Two-sum of a float into (hi, lo).
-__device__ __forceinline__ void df_add(float &hi, float &lo, float x) {
-  float s = hi + x;
-  float bp = s - hi;
-  float e = (hi - (s - bp)) + (x - bp);
-  hi = s;
-  lo += e;
-}
-
-// Add |v|^2 of an FP32 amplitude into (hi, lo) without rounding the
-// squares: x*x = p + e exactly with e = fma(x, x, -p).  The error terms of
-// the squares and of the two-sums are gathered in lo.
-__device__ __forceinline__ void df_add_prob(float &hi, float &lo, float2 v) {
-  float pr = v.x * v.x, er = fmaf(v.x, v.x, -pr);
-  float pi = v.y * v.y, ei = fmaf(v.y, v.y, -pi);
-  float s = pr + pi;
-  float bp = s - pr;
-  float es = (pr - (s - bp)) + (pi - bp);
-  df_add(hi, lo, s);
-  lo += (er + ei) + es;
-}
-
-// |v|^2 as a double for an FP32 amplitude: exact squares, rounded once.
-__device__ __forceinline__ double prob_f64(float2 v) {
-  float hi = 0.f, lo = 0.f;
-  df_add_prob(hi, lo, v);
-  return (double)hi + (double)lo;
-}
-__device__ __forceinline__ double prob_f64(double2 v) { return fma(v.x, v.x, v.y * v.y); }
-
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -271,7 +239,10 @@ __global__ void __launch_bounds__(256)
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t t = warp; t < nshots; t += nwarps) {
-    const double p = draws[t];
+    // FP32 states sample the renormalised distribution: their norm drifts by
+    // ~1e-7 over a deep circuit, which would shift the whole CDF; FP64 states
+    // use the draw as is, like the reference.
+    const double p = sizeof(T) == 4 ? draws[t] * prefix[nblocks - 1] : draws[t];
     // First block whose inclusive prefix passes p.
     uint64_t lo = 0, hi = nblocks;  // search in [lo, hi)
     while (lo < hi) {
@@ -330,13 +301,14 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// sum conj(a_i) b_i and max |a_i - b_i| over two states of equal length.
+// sum conj(a_i) b_i, max |a_i - b_i|, |a|^2 and |b|^2 over two states of
+// equal length: 5 partials per block.
 template <typename TA, typename TB>
 __global__ void __launch_bounds__(kReduceThreads)
     k_inner(const typename CT<TA>::C *__restrict__ a, const typename CT<TB>::C *__restrict__ b,
             uint64_t len, double *__restrict__ partials) {
   __shared__ double sh[kReduceThreads / 32];
-  double re = 0.0, im = 0.0, mx = 0.0;
+  double re = 0.0, im = 0.0, mx = 0.0, na = 0.0, nb = 0.0;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
        i += (uint64_t)gridDim.x * blockDim.x) {
     typename CT<TA>::C x = a[i];
@@ -344,11 +316,15 @@ __global__ void __launch_bounds__(kReduceThreads)
     double xr = x.x, xi = x.y, yr = y.x, yi = y.y;
     re += xr * yr + xi * yi;
     im += xr * yi - xi * yr;
+    na += xr * xr + xi * xi;
+    nb += yr * yr + yi * yi;
     double dr = xr - yr, di = xi - yi;
     mx = fmax(mx, sqrt(dr * dr + di * di));
   }
   double r = block_sum<kReduceThreads>(re, sh);
   double s = block_sum<kReduceThreads>(im, sh);
+  double sa = block_sum<kReduceThreads>(na, sh);
+  double sb = block_sum<kReduceThreads>(nb, sh);
   // block max
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -360,9 +336,12 @@ __global__ void __launch_bounds__(kReduceThreads)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if (lane == 0) {
-      partials[3 * blockIdx.x] = r;
-      partials[3 * blockIdx.x + 1] = s;
-      partials[3 * blockIdx.x + 2] = m;
+      double *q = partials + 5 * blockIdx.x;
+      q[0] = r;
+      q[1] = s;
+      q[2] = m;
+      q[3] = sa;
+      q[4] = sb;
     }
   }
 }
@@ -370,15 +349,20 @@ __global__ void __launch_bounds__(kReduceThreads)
 __global__ void k_finish_inner(const double *__restrict__ partials, int nparts,
                                MeasResult *__restrict__ res) {
   // single thread, fixed order (nparts is small)
-  double re = 0.0, im = 0.0, mx = 0.0;
+  double re = 0.0, im = 0.0, mx = 0.0, na = 0.0, nb = 0.0;
   for (int i = 0; i < nparts; ++i) {
-    re += partials[3 * i];
-    im += partials[3 * i + 1];
-    mx = fmax(mx, partials[3 * i + 2]);
+    const double *q = partials + 5 * i;
+    re += q[0];
+    im += q[1];
+    mx = fmax(mx, q[2]);
+    na += q[3];
+    nb += q[4];
   }
   res->prob = re;
   res->aux = im;
   res->inv_norm = mx;
+  res->na = na;
+  res->nb = nb;
 }
 
 // ---- host helpers ---------------------------------------------------------------------
@@ -466,7 +450,7 @@ static int sample_device(qvmg_state s, const double *d_draws, uint64_t nshots, i
 static int inner_impl(qvmg_state a, qvmg_state b) {
   int rc = order_states(a, b);
   if (rc) return rc;
-  if ((rc = ensure_dvec(a, 3 * kReduceBlocks * sizeof(double)))) return rc;
+  if ((rc = ensure_dvec(a, 5 * kReduceBlocks * sizeof(double)))) return rc;
   double *parts = a->dvec;
   auto go = [&](auto ta, auto tb) {
     using TA = decltype(ta);
@@ -658,7 +642,8 @@ int qvmg_fidelity(qvmg_state a, qvmg_state b, double *fidelity, double *max_abs_
   if (a->nq != b->nq) return fail(QVMG_E_INVALID, "fidelity of states of different sizes");
   if ((rc = inner_impl(a, b))) return rc;
   double re = a->hres->prob, im = a->hres->aux;
-  if (fidelity) *fidelity = re * re + im * im;
+  // fidelity of the normalised states: |<a|b>|^2 / (<a|a><b|b>)
+  if (fidelity) *fidelity = (re * re + im * im) / (a->hres->na * a->hres->nb);
   if (max_abs_err) *max_abs_err = a->hres->inv_norm;
   return QVMG_OK;
 }

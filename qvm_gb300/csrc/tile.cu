@@ -163,7 +163,8 @@ __global__ void __launch_bounds__(kTileThreads)
   C *tile = reinterpret_cast<C *>(smem);
   unsigned long long *rowoff = reinterpret_cast<unsigned long long *>(tile + (1u << t));
   const unsigned nrows = 1u << (t - L);
-  C *data = reinterpret_cast<C *>(rowoff + nrows);
+  // row offsets padded to 16 bytes so that double2 op data stays aligned
+  C *data = reinterpret_cast<C *>(rowoff + ((nrows + 1u) & ~1u));
   TileOpDev *ops = reinterpret_cast<TileOpDev *>(data + p.ndata);
   {
     const C *gd = reinterpret_cast<const C *>(p.data);
@@ -231,7 +232,8 @@ __global__ void __launch_bounds__(kTileThreads)
 
 size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops) {
   size_t csz = prec == QVMG_FP64 ? 16 : 8;
-  size_t b = ((size_t)1 << t) * csz + ((size_t)1 << (t - L)) * 8 + (size_t)ndata * csz +
+  size_t rows = ((size_t)1 << (t - L)) + 1 & ~(size_t)1;  // padded to 16 bytes
+  size_t b = ((size_t)1 << t) * csz + rows * 8 + (size_t)ndata * csz +
              (size_t)nops * sizeof(TileOpDev);
   return (b + 15) & ~(size_t)15;
 }

@@ -129,12 +129,14 @@ def test_sample_matches_oracle(gpu, oracle, prec, rule):
         s = upload(wf, prec)
         draws = rng.random(512)
         got = s.sample(draws, rule=rule)
+        # FP32 states sample the renormalised distribution (draw x total)
+        eff = draws if prec == "fp64" else draws * np.sum(np.abs(ref) ** 2)
         if rule == "bisect":
-            want = np.array([oracle.sample_bisect(ref, p) for p in draws])
+            want = np.array([oracle.sample_bisect(ref, p) for p in eff])
         else:
-            want = oracle.sample_multiple(ref, draws)
+            want = oracle.sample_multiple(ref, eff)
         cdf = np.cumsum(np.abs(ref) ** 2)
-        ok = (got == want) | near_boundary(cdf, draws)
+        ok = (got == want) | near_boundary(cdf, eff)
         assert ok.all(), (n, np.nonzero(~ok))
         s.free()
 
