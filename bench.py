@@ -44,8 +44,8 @@ def parse():
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--shots", type=int, default=4096)
-    ap.add_argument("--fw", type=int, default=2)
-    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--fw", type=int, default=0, help="fusion width (0: autotune)")
+    ap.add_argument("--tile", type=int, default=0, help="tile qubits (0: autotune)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -57,6 +57,23 @@ def dist():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def max_over_ranks(value: float) -> float:
+    """The slowest rank's time (all_reduce MAX; NCCL on GPUs, gloo on CPU)."""
+    import torch
+    import torch.distributed as tdist
+    if not tdist.is_initialized() or tdist.get_world_size() == 1:
+        return float(value)
+    dev = "cuda" if tdist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank_step: int, steps: int, world: int, max_ms: float) -> float:
+    """Units all ranks processed divided by the slowest rank's time."""
+    return world * units_per_rank_step * steps / (max_ms / 1e3)
 
 
 def peaks():
@@ -190,9 +207,17 @@ def main():
     G = len(gates)
     prog = Program()
     prog.add_gates(gates)
-    stats = prog.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
     s32 = CudaPureState(n, "fp32")
     stream = torch.cuda.ExternalStream(s32.stream())
+    tuned = None
+    if args.fw == 0 or args.tile == 0:
+        # untimed: pick fusion width and tile width for this circuit on this GPU
+        from qvm_gb300.autotune import DEFAULT_CANDIDATES, autotune
+        cands = [(fw, t) for fw, t in DEFAULT_CANDIDATES["fp32"]
+                 if (args.fw in (0, fw)) and (args.tile in (0, t))]
+        (args.fw, args.tile), table = autotune(prog, s32, "fp32", cands)
+        tuned = {f"fw{fw}_t{t}": round(ms, 2) for (fw, t), ms in sorted(table.items())}
+    stats = prog.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
 
     def step():
         s32.set_to_zero_state()
@@ -226,11 +251,8 @@ def main():
     torch.cuda.synchronize()
     total_ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = ws * G * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(total_ms)
+    value = whole_job_rate(G, args.steps, ws, total_ms)
 
     result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -241,6 +263,7 @@ def main():
         "workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth {args.depth}, {G} gates, "
                     f"fused FP32 (fusion width {args.fw})",
         "passes": stats["passes"], "fused_blocks": stats["fused_blocks"],
+        "fusion_width": args.fw, "tile_qubits": args.tile, "autotune_ms": tuned,
         "state_bytes": state_bytes,
         "l2": "state (%.1f GiB) is larger than L2; no flush needed" % (state_bytes / 2 ** 30),
         "parallelism": f"replicas x{ws}"}

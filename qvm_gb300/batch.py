@@ -1,0 +1,93 @@
+"""Batched QAOA MaxCut instances (one persistent launch for many circuits).
+
+Mirrors the QAOA workload of the reference's examples/qaoa.lisp:7-206 (H on
+all qubits, p layers of ZZ(gamma) on graph edges and RX(2 beta) on all
+qubits; sampling with sample-wavefunction-multiple-times), for batches of
+uneven instances held on the device.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+
+class QaoaBatch:
+    def __init__(self, graphs, gammas, betas):
+        """graphs: list of (n, edges); gammas, betas: (ninst, p) arrays."""
+        self.ninst = len(graphs)
+        g = np.ascontiguousarray(gammas, dtype=np.float64).reshape(self.ninst, -1)
+        b = np.ascontiguousarray(betas, dtype=np.float64).reshape(self.ninst, -1)
+        if g.shape != b.shape:
+            raise ValueError("gammas and betas must have the same shape")
+        self.p = g.shape[1]
+        self.n = np.array([int(n) for n, _ in graphs], dtype=np.int32)
+        ne = np.array([len(e) for _, e in graphs], dtype=np.int32)
+        flat = np.array([x for _, e in graphs for uv in e for x in uv], dtype=np.int32)
+        if flat.size == 0:
+            flat = np.zeros(2, dtype=np.int32)
+        self.graphs = [(int(n), [tuple(map(int, uv)) for uv in e]) for n, e in graphs]
+        self._h = ctypes.c_void_p()
+        ip = ctypes.POINTER(ctypes.c_int)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.call("qvmg_qaoa_batch_create", self.ninst, self.n.ctypes.data_as(ip),
+               ne.ctypes.data_as(ip), flat.ctypes.data_as(ip), self.p, g.ctypes.data_as(dp),
+               b.ctypes.data_as(dp), ctypes.byref(self._h))
+
+    def set_angles(self, gammas, betas):
+        g = np.ascontiguousarray(gammas, dtype=np.float64).reshape(self.ninst, self.p)
+        b = np.ascontiguousarray(betas, dtype=np.float64).reshape(self.ninst, self.p)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.call("qvmg_qaoa_batch_set_angles", self._h, g.ctypes.data_as(dp), b.ctypes.data_as(dp))
+
+    def run(self, draws=None):
+        """Returns (expectations[ninst], shots[ninst, nshots] or None)."""
+        dp = ctypes.POINTER(ctypes.c_double)
+        ex = np.zeros(self.ninst, dtype=np.float64)
+        if draws is None:
+            L.call("qvmg_qaoa_batch_run", self._h, None, 0, ex.ctypes.data_as(dp), None)
+            return ex, None
+        d = np.ascontiguousarray(draws, dtype=np.float64).reshape(self.ninst, -1)
+        shots = np.zeros(d.shape, dtype=np.uint32)
+        L.call("qvmg_qaoa_batch_run", self._h, d.ctypes.data_as(dp), d.shape[1],
+               ex.ctypes.data_as(dp), shots.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        return ex, shots
+
+    def state(self, i: int) -> np.ndarray:
+        out = np.zeros(1 << int(self.n[i]), dtype=np.complex128)
+        L.call("qvmg_qaoa_batch_state", self._h, int(i),
+               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return out
+
+    def device_bytes(self) -> int:
+        return int(L.lib().qvmg_qaoa_batch_bytes(self._h))
+
+    def free(self):
+        if self._h:
+            L.call("qvmg_qaoa_batch_free", self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def random_qaoa_batch(ngraphs: int, sizes, params_per_graph: int, p: int, seed: int = 4):
+    """The batched QAOA workload: random 3-regular graphs with n drawn from
+    `sizes`, each with `params_per_graph` (gamma, beta) sets drawn uniformly
+    from [0, pi) x [0, pi/2); returns (graphs, gammas, betas)."""
+    from .circuits import random_3_regular_graph
+    rng = np.random.default_rng(seed)
+    graphs, gam, bet = [], [], []
+    for _ in range(ngraphs):
+        n = int(rng.choice(sizes))
+        edges = random_3_regular_graph(n, rng)
+        for _ in range(params_per_graph):
+            graphs.append((n, edges))
+            gam.append(rng.uniform(0, np.pi, p))
+            bet.append(rng.uniform(0, np.pi / 2, p))
+    return graphs, np.array(gam), np.array(bet)

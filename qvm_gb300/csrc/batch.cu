@@ -252,7 +252,8 @@ __global__ void __launch_bounds__(kQaoaThreads) k_qaoa_batch(const __grid_consta
     __syncthreads();
     // shots: smallest x with C(x) >= draw (src/measurement.lisp:246-288), len-1 if none
     for (int t = warp; t < A.nshots; t += nwarps) {
-      const double p = A.draws[(unsigned long long)I.id * A.nshots + t];
+      // renormalised FP32 distribution, as in qvmg_sample
+      const double p = A.draws[(unsigned long long)I.id * A.nshots + t] * sub[nsub - 1];
       unsigned long long lo = 0, hi = nsub;
       while (lo < hi) {
         unsigned long long mid = (lo + hi) >> 1;

@@ -23,6 +23,16 @@
 
 namespace qvmg {
 
+// 16-byte asynchronous global -> shared copy (LDGSTS): every load of a tile
+// is in flight at once without holding registers; wait_all completes them.
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 __device__ __forceinline__ unsigned inject0u(unsigned x, int q) {
   unsigned lo = x & ((1u << q) - 1u);
   return ((x >> q) << (q + 1)) | lo;
@@ -155,7 +165,7 @@ __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
 // KMAX: widest op of the pass; narrower instantiations keep the register
 // arrays of the wide cases out of the kernel (no spills for k <= 2).
 template <typename T, int KMAX>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, KMAX <= 2 ? 3 : 1)
     k_tile(typename CT<T>::C *__restrict__ a, const __grid_constant__ TileArgs p) {
   using C = typename CT<T>::C;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -195,8 +205,9 @@ __global__ void __launch_bounds__(kTileThreads)
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
       const int4 *src = reinterpret_cast<const int4 *>(a + rowoff[el >> L] + (el & rowmask));
-      reinterpret_cast<int4 *>(tile)[ch] = __ldcs(src);
+      cp_async16(reinterpret_cast<int4 *>(tile) + ch, src);
     }
+    cp_async_wait_all();
     __syncthreads();
     for (int o = 0; o < p.nops; ++o) {
       const TileOpDev &op = ops[o];
@@ -239,34 +250,39 @@ size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops) {
 }
 
 template <typename T, int KMAX>
-static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem, unsigned grid) {
+static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
   static bool attr = false;  // per instantiation
   if (!attr) {
     QVMG_CUDA(cudaFuncSetAttribute(k_tile<T, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    kTileMaxSmem));
     attr = true;
   }
-  k_tile<T, KMAX><<<grid, kTileThreads, smem, s->stream>>>((typename CT<T>::C *)s->amps, args);
+  // Persistent grid: as many CTAs as fit on every SM at once (registers and
+  // shared memory), each looping over tiles.
+  int per_sm = 0;
+  QVMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<T, KMAX>, kTileThreads,
+                                                          smem));
+  if (per_sm < 1) return fail(QVMG_E_UNSUPPORTED, "tile pass does not fit on an SM");
+  uint64_t grid = std::min<uint64_t>(args.ntiles, (uint64_t)sm_count() * per_sm);
+  k_tile<T, KMAX><<<(unsigned)grid, kTileThreads, smem, s->stream>>>(
+      (typename CT<T>::C *)s->amps, args);
   QVMG_CHECK_LAUNCH("k_tile");
   return QVMG_OK;
 }
 
 template <typename T>
-static int tile_launch(qvmg_state s, const TileArgs &args, size_t smem, unsigned grid) {
-  if (args.kmax <= 2) return tile_launch_k<T, 2>(s, args, smem, grid);
-  if (args.kmax <= 3) return tile_launch_k<T, 3>(s, args, smem, grid);
-  return tile_launch_k<T, 5>(s, args, smem, grid);
+static int tile_launch(qvmg_state s, const TileArgs &args, size_t smem) {
+  if (args.kmax <= 2) return tile_launch_k<T, 2>(s, args, smem);
+  if (args.kmax <= 3) return tile_launch_k<T, 3>(s, args, smem);
+  return tile_launch_k<T, 5>(s, args, smem);
 }
 
 int launch_tile(qvmg_state s, const TileArgs &args) {
   size_t smem = tile_smem_bytes(s->prec, args.t, args.L, args.ndata, args.nops);
   if (smem > (size_t)kTileMaxSmem) return fail(QVMG_E_UNSUPPORTED, "tile pass exceeds shared memory");
   if (args.kmax < 1 || args.kmax > 5) return fail(QVMG_E_INVALID, "tile op width out of range");
-  int per_sm = std::max(1, (int)((size_t)(kTileMaxSmem + 1024) / (smem + 1024)));
-  per_sm = std::min(per_sm, 2048 / kTileThreads);
-  uint64_t grid = std::min<uint64_t>(args.ntiles, (uint64_t)sm_count() * per_sm);
-  if (s->prec == QVMG_FP64) return tile_launch<double>(s, args, smem, (unsigned)grid);
-  return tile_launch<float>(s, args, smem, (unsigned)grid);
+  if (s->prec == QVMG_FP64) return tile_launch<double>(s, args, smem);
+  return tile_launch<float>(s, args, smem);
 }
 
 }  // namespace qvmg

@@ -6,7 +6,7 @@
 
 namespace qvmg {
 
-constexpr int kTileThreads = 512;
+constexpr int kTileThreads = 256;
 constexpr int kTileMaxSmem = 227 * 1024;
 constexpr int kTileMaxE = 24;
 

@@ -1,0 +1,215 @@
+"""Continuous-batching request engine for the statevector path.
+
+The reference's server (app/src/entry-point.lisp:655-673,
+app/src/handle-request.lisp:44-187) runs one thread per HTTP connection,
+each building its own QVM, with no batching across requests and a full GC
+per request to release foreign memory.  Here requests are admitted onto the
+GPU by HBM bytes (16*2^n for FP64, 8*2^n for FP32, plus scratch) within a
+budget; every admitted request runs on its own state and CUDA stream, so the
+device overlaps the work of many requests; a request that arrives while
+others run is admitted as soon as a worker and enough memory are free
+(first fit from the queue, so a small request is not stuck behind a large
+one).  Freed states are kept in a pool keyed by (qubits, precision) and
+reused, evicted least-recently-used when admission needs their bytes.
+
+Each request's result depends only on its own program and draws: states are
+reset before use and every kernel is deterministic, so a request returns the
+same shots alone and in the mix.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .state import CudaPureState, Program, state_bytes
+
+
+@dataclass
+class Request:
+    n: int
+    gates: list                   # (matrix, nat-tuple qubits) pairs
+    shots: int
+    precision: str = "fp32"
+    draws: np.ndarray | None = None
+    fused: bool = True
+    tag: str = ""
+    arrival: float = field(default_factory=time.perf_counter)
+
+
+@dataclass
+class Result:
+    shots: np.ndarray
+    queued_s: float
+    run_s: float
+    latency_s: float
+    tag: str = ""
+
+
+class StatePool:
+    """Idle device states by (n, precision), least recently used first."""
+
+    def __init__(self):
+        self.idle = collections.OrderedDict()  # key -> list of states
+
+    def take(self, n, prec):
+        lst = self.idle.get((n, prec))
+        if lst:
+            s = lst.pop()
+            if not lst:
+                del self.idle[(n, prec)]
+            return s
+        return None
+
+    def give(self, s: CudaPureState, prec):
+        key = (s.num_qubits(), prec)
+        self.idle.setdefault(key, []).append(s)
+        self.idle.move_to_end(key)
+
+    def evict_one(self) -> int:
+        """Free the least recently used idle state; returns its bytes (0 if none)."""
+        if not self.idle:
+            return 0
+        key = next(iter(self.idle))
+        lst = self.idle[key]
+        s = lst.pop(0)
+        if not lst:
+            del self.idle[key]
+        b = state_bytes(key[0], key[1])
+        s.free()
+        return b
+
+    def bytes(self) -> int:
+        return sum(state_bytes(k[0], k[1]) * len(v) for k, v in self.idle.items())
+
+
+class Server:
+    def __init__(self, hbm_budget: float = 180e9, workers: int = 16):
+        self.budget = int(hbm_budget)
+        self.reserved = 0              # bytes of running requests + idle pooled states
+        self.pool = StatePool()
+        self.queue = collections.deque()
+        self.cv = threading.Condition()
+        self.stop = False
+        self.threads = [threading.Thread(target=self._worker, daemon=True) for _ in range(workers)]
+        for t in self.threads:
+            t.start()
+
+    def submit(self, req: Request) -> Future:
+        need = state_bytes(req.n, req.precision)
+        if need == 0 or need > self.budget:
+            raise ValueError(f"a {req.n}-qubit {req.precision} state does not fit the "
+                             f"{self.budget} byte budget")
+        fut = Future()
+        with self.cv:
+            self.queue.append((req, fut, need))
+            self.cv.notify()
+        return fut
+
+    def _admit(self):
+        """First queued request that fits (evicting idle pooled states if that
+        makes it fit).  Called with the lock held."""
+        for i, (req, fut, need) in enumerate(self.queue):
+            key_state = self.pool.take(req.n, req.precision)
+            if key_state is not None:
+                del self.queue[i]
+                return req, fut, need, key_state   # its bytes are already reserved
+            while self.reserved + need > self.budget:
+                freed = self.pool.evict_one()
+                if freed == 0:
+                    break
+                self.reserved -= freed
+            if self.reserved + need <= self.budget:
+                del self.queue[i]
+                self.reserved += need
+                return req, fut, need, None
+        return None
+
+    def _worker(self):
+        while True:
+            with self.cv:
+                item = None
+                while not self.stop:
+                    item = self._admit()
+                    if item is not None:
+                        break
+                    self.cv.wait()
+                if item is None:
+                    return
+            req, fut, need, st = item
+            t0 = time.perf_counter()
+            try:
+                if st is None:
+                    st = CudaPureState(req.n, req.precision)
+                else:
+                    st.set_to_zero_state()
+                prog = Program()
+                prog.add_gates(req.gates)
+                if req.fused:
+                    prog.plan(req.n, req.precision, fused=True, fusion_width=2)
+                prog.run(st, fused=req.fused)
+                draws = req.draws
+                if draws is None:
+                    draws = np.random.default_rng(0).random(req.shots)
+                shots = st.sample(draws)
+                prog.free()
+                t1 = time.perf_counter()
+                fut.set_result(Result(shots, t0 - req.arrival, t1 - t0, t1 - req.arrival, req.tag))
+            except Exception as e:  # the request fails, the server keeps going
+                fut.set_exception(e)
+                if st is not None:
+                    st.free()
+                    st = None
+            with self.cv:
+                if st is not None:
+                    self.pool.give(st, req.precision)   # stays reserved while pooled
+                else:
+                    self.reserved -= need
+                self.cv.notify_all()
+
+    def close(self):
+        with self.cv:
+            self.stop = True
+            self.cv.notify_all()
+        for t in self.threads:
+            t.join()
+        with self.cv:
+            while self.pool.evict_one():
+                pass
+            self.reserved = 0
+
+
+def serving_workload(duration_s: float, rate: float = 200.0, seed: int = 5,
+                     nmin: int = 10, nmax: int = 30, depth=(5, 40)):
+    """The serving stream: Poisson arrivals, qubit counts uniform in
+    [nmin, nmax], programs drawn from the random-layer family, the QFT and
+    QAOA MaxCut (depth uniform in `depth`), shots log-uniform in 1..10^4,
+    FP32 or FP64 per request.  Returns [(arrival_offset_s, Request)]."""
+    from . import circuits
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration_s:
+            return out
+        n = int(rng.integers(nmin, nmax + 1))
+        fam = ["layers", "qft", "qaoa"][int(rng.integers(3))]
+        d = int(rng.integers(depth[0], depth[1] + 1))
+        if fam == "layers":
+            gates = circuits.random_layers(n, layers=d, seed=int(rng.integers(1 << 30)))
+        elif fam == "qft":
+            gates = circuits.qft(n)
+        else:
+            m = n if n % 2 == 0 else n - 1
+            edges = circuits.random_3_regular_graph(m, rng)
+            p = max(1, d // 10)
+            gates = circuits.qaoa_maxcut(m, edges, rng.uniform(0, np.pi, p),
+                                         rng.uniform(0, np.pi / 2, p))
+        shots = int(np.exp(rng.uniform(0, np.log(1e4))))
+        prec = "fp32" if rng.random() < 0.5 else "fp64"
+        draws = rng.random(shots)
+        out.append((t, Request(n, gates, shots, prec, draws, True, f"{fam}-{n}-{prec}")))

@@ -88,8 +88,10 @@ def test_measure_matches_oracle(gpu, oracle, prec, compiled):
             wused = True
         else:
             wbit, wused, wprob = oracle.measure(want, int(q), draw)
-        assert abs(prob - wprob) < 1e-12
-        if abs(draw - wprob) > 1e-12:
+        # FP32 collapses renormalise in FP32: later probabilities drift ~1e-8
+        ptol = 1e-12 if prec == "fp64" else 1e-6
+        assert abs(prob - wprob) < ptol
+        if abs(draw - wprob) > ptol:
             assert bit == wbit and used == wused
         tol = 1e-12 if prec == "fp64" else 2e-6
         assert np.max(np.abs(s.state_elements() - want)) < tol

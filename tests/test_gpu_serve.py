@@ -1,0 +1,54 @@
+"""GPU: the continuous-batching engine returns the same result for a request
+alone and in a concurrent mix, and respects its HBM admission budget."""
+import numpy as np
+import pytest
+
+from qvm_gb300 import circuits
+from qvm_gb300.serve import Request, Server
+from qvm_gb300.state import state_bytes
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    rng = np.random.default_rng(9)
+    reqs = []
+    for i in range(24):
+        n = int(rng.integers(10, 21))
+        fam = i % 3
+        if fam == 0:
+            gates = circuits.random_layers(n, layers=int(rng.integers(2, 8)), seed=i)
+        elif fam == 1:
+            gates = circuits.qft(n)
+        else:
+            m = n - (n % 2)
+            e = circuits.random_3_regular_graph(m, rng)
+            gates = circuits.qaoa_maxcut(m, e, [0.4, 0.9], [0.3, 0.2])
+        prec = "fp32" if i % 2 else "fp64"
+        shots = int(rng.integers(1, 2000))
+        reqs.append(Request(n, gates, shots, prec, rng.random(shots), True, f"r{i}"))
+    return reqs
+
+
+def test_same_result_alone_and_in_mix(gpu):
+    reqs = _requests()
+    alone = {}
+    srv = Server(hbm_budget=8e9, workers=1)
+    for r in reqs:
+        alone[r.tag] = srv.submit(r).result().shots
+    srv.close()
+    # the mix: many workers, a tight budget that forces admission waits
+    budget = max(state_bytes(r.n, r.precision) for r in reqs) * 3
+    srv = Server(hbm_budget=budget, workers=8)
+    futs = [(r.tag, srv.submit(r)) for r in reqs]
+    for tag, f in futs:
+        np.testing.assert_array_equal(f.result().shots, alone[tag])
+        assert srv.reserved <= budget
+    srv.close()
+
+
+def test_oversized_request_rejected(gpu):
+    srv = Server(hbm_budget=1e6, workers=1)
+    with pytest.raises(ValueError):
+        srv.submit(Request(20, circuits.qft(20), 1, "fp64"))
+    srv.close()
