@@ -142,6 +142,28 @@ int qvmg_measure_all(qvmg_state s, double draw, uint64_t *index);
  * (sample-wavefunction-multiple-times, src/measurement.lisp:246-288). */
 int qvmg_sample(qvmg_state s, const double *draws, uint64_t nshots, int rule,
                 uint64_t *out);
+/* Multishot sampling that allocates nothing.  This entry point has no
+ * counterpart in the reference: it serves callers that cannot allocate
+ * device memory -- a host that owns the whole device pool and hands out
+ * slices of it, or a latency-critical loop that cannot afford cudaMalloc's
+ * implicit synchronisation -- and so cannot create a qvmg_state.  The caller
+ * passes device pointers: `amps` (2^nqubits amplitudes, double2 for
+ * QVMG_FP64 or float2 for QVMG_FP32, LSB-first), `draws` (nshots doubles in
+ * [0, 1]) and `out` (nshots uint64 indices), plus the cudaStream_t to order
+ * the work on (NULL = the default stream).  The call only queues work; the
+ * results are in `out` once that stream reaches them.  Results equal
+ * qvmg_sample's for the same amplitudes, draws and rule.
+ *  - Limit: nqubits <= 30.  The CDF block sums live in a fixed 2 MiB device
+ *    array (2^18 + 1 doubles) that every GPU which loads this library holds
+ *    until the process exits; larger states are rejected with
+ *    QVMG_E_INVALID.
+ *  - The first call on a device looks up that array's device address (once
+ *    per device); make that first call before any CUDA stream capture.
+ *  - All calls share the one array.  Each call overwrites every entry it
+ *    reads before reading it, but calls whose work overlaps on the GPU (on
+ *    different streams, or from different threads) race on it: order them. */
+int qvmg_sample_noalloc(const void *amps, int nqubits, int precision, const double *draws,
+                        uint64_t nshots, int rule, uint64_t *out, void *stream);
 /* |a_i|^2 for every amplitude (app/src/api/probabilities.lisp:13-19). */
 int qvmg_probabilities(qvmg_state s, double *out);
 /* norm / normalize-wavefunction (src/wavefunction.lisp:332-364). */

@@ -52,6 +52,7 @@ SIGNATURES = {
     "qvmg_measure": (_i, [_vp, _i, ctypes.c_double, _i, _ip, _ip, _dp]),
     "qvmg_measure_all": (_i, [_vp, ctypes.c_double, _u64p]),
     "qvmg_sample": (_i, [_vp, _dp, _u64, _i, _u64p]),
+    "qvmg_sample_noalloc": (_i, [_vp, _i, _i, _vp, _u64, _i, _vp, _vp]),
     "qvmg_probabilities": (_i, [_vp, _dp]),
     "qvmg_norm": (_i, [_vp, _dp]),
     "qvmg_normalize": (_i, [_vp]),

@@ -24,6 +24,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -649,3 +650,92 @@ int qvmg_fidelity(qvmg_state a, qvmg_state b, double *fidelity, double *max_abs_
 }
 
 }  // extern "C"
+
+// ---- sampling without any allocation ----------------------------------------------
+//
+// qvmg_sample needs a state handle, and creating one allocates device memory
+// (the amplitudes and the per-state CDF scratch).  Some callers cannot do
+// that: a host that hands the library a slice of its own pre-reserved device
+// pool and forbids cudaMalloc (which synchronises the device and can fail
+// under memory pressure in a long-running server), or a caller in the middle
+// of a latency-critical loop where an allocation's implicit synchronisation
+// is not acceptable.  qvmg_sample_noalloc serves them: the caller passes the
+// amplitudes, the draws and the output as device pointers plus a stream, and
+// the block sums of the two-level CDF live in the fixed array below, which
+// every GPU that loads this library holds until the process exits.
+namespace qvmg {
+
+// Largest state the fixed scratch covers: 2^30 amplitudes.
+constexpr int kNoAllocMaxQubits = 30;
+constexpr uint64_t kNoAllocBlocks = 1ull << (kNoAllocMaxQubits - kSampleBlockBits);
+
+// Block sums of the CDF (then their inclusive prefix), shared by all calls.
+static __device__ __align__(256) double g_noalloc_cdf[kNoAllocBlocks + 1];
+
+// Device address of g_noalloc_cdf per device ordinal, looked up once.
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[256];
+
+static int noalloc_scratch(double **out) {
+  int dev = 0;
+  QVMG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail(QVMG_E_UNSUPPORTED, "device ordinal out of range");
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_cdf);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_cdf)");
+    g_noalloc_ptr[dev] = (double *)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return QVMG_OK;
+}
+
+template <typename T>
+static int sample_noalloc_impl(const void *amps, int n, const double *draws, uint64_t nshots,
+                               int rule, unsigned long long *out, double *cdf,
+                               cudaStream_t st) {
+  using C = typename CT<T>::C;
+  const uint64_t len = 1ull << n;
+  const int bb = n > kSampleBlockBits ? kSampleBlockBits : n;
+  const uint64_t nblocks = len >> bb;
+  // Every entry of cdf[0..nblocks) is written by k_block_sums before the scan
+  // reads it, so nothing left over from an earlier call is ever used.
+  int grid = (int)std::min<uint64_t>(nblocks, (uint64_t)sm_count() * 8);
+  k_block_sums<T><<<grid, 256, 0, st>>>((const C *)amps, nblocks, bb, cdf);
+  QVMG_CHECK_LAUNCH("k_block_sums");
+  k_scan_inclusive<<<1, 1024, 0, st>>>(cdf, nblocks);
+  QVMG_CHECK_LAUNCH("k_scan_inclusive");
+  k_sample<T><<<grid_for(nshots * 32, 256), 256, 0, st>>>((const C *)amps, len, bb, cdf, nblocks,
+                                                          draws, nshots, rule, out);
+  QVMG_CHECK_LAUNCH("k_sample");
+  return QVMG_OK;
+}
+
+}  // namespace qvmg
+
+extern "C" int qvmg_sample_noalloc(const void *amps, int nqubits, int precision,
+                                   const double *draws, uint64_t nshots, int rule,
+                                   uint64_t *out, void *stream) {
+  if (nqubits < 1 || nqubits > kNoAllocMaxQubits)
+    return fail(QVMG_E_INVALID, "qvmg_sample_noalloc: " + std::to_string(nqubits) +
+                                    " qubits is outside 1.." +
+                                    std::to_string(kNoAllocMaxQubits) +
+                                    ", the size its fixed scratch covers");
+  if (precision != QVMG_FP64 && precision != QVMG_FP32)
+    return fail(QVMG_E_INVALID, "qvmg_sample_noalloc: precision must be QVMG_FP64 or QVMG_FP32");
+  if (rule != QVMG_SAMPLE_BISECT && rule != QVMG_SAMPLE_CDF)
+    return fail(QVMG_E_INVALID, "qvmg_sample_noalloc: unknown sampling rule");
+  if (nshots == 0) return QVMG_OK;
+  if (!amps || !draws || !out)
+    return fail(QVMG_E_INVALID, "qvmg_sample_noalloc: null device pointer");
+  double *cdf = nullptr;
+  int rc = noalloc_scratch(&cdf);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == QVMG_FP64)
+    return sample_noalloc_impl<double>(amps, nqubits, draws, nshots, rule,
+                                       (unsigned long long *)out, cdf, st);
+  return sample_noalloc_impl<float>(amps, nqubits, draws, nshots, rule,
+                                    (unsigned long long *)out, cdf, st);
+}
