@@ -46,8 +46,11 @@ def parse():
     ap.add_argument("--shots", type=int, default=4096)
     ap.add_argument("--fw", type=int, default=0, help="fusion width (0: autotune)")
     ap.add_argument("--tile", type=int, default=0, help="tile qubits (0: autotune)")
+    ap.add_argument("--reg", type=int, default=-1, help="register stages 0/1 (-1: autotune)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched QAOA run")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -160,6 +163,69 @@ def cpu_baseline(n, gates, seconds, threads):
                       f"{dt:.1f} s"}
 
 
+def run_qaoa_batch(seed: int = 4, runs: int = 3):
+    """Batched QAOA MaxCut: 512 random 3-regular graphs with n in {12..22},
+    8 (gamma, beta) sets each = 4096 instances, p = 4, 1024 shots each, one
+    persistent launch per run (CUDA graph).  Timed end to end per run, with
+    the draws' upload and the shots' and expectations' download."""
+    from qvm_gb300.batch import QaoaBatch, random_qaoa_batch
+    graphs, gam, bet = random_qaoa_batch(512, [12, 14, 16, 18, 20, 22], 8, p=4, seed=seed)
+    b = QaoaBatch(graphs, gam, bet)
+    draws = np.random.default_rng(seed).random((len(graphs), 1024))
+    ex, shots = b.run(draws)  # warm-up (graph capture)
+    times = []
+    for _ in range(runs):
+        t0 = time.perf_counter()
+        ex, shots = b.run(draws)
+        times.append(time.perf_counter() - t0)
+    ngates = sum(n + 4 * (len(e) + n) for n, e in graphs)
+    dt = float(np.median(times))
+    out = {"instances": len(graphs), "qubits": "12..22", "p": 4, "shots_per_instance": 1024,
+           "ms_per_batch": 1e3 * dt, "instances_per_s": len(graphs) / dt,
+           "gates_per_s": ngates / dt, "device_gib": b.device_bytes() / 2 ** 30,
+           "expectation_mean": float(np.mean(ex)),
+           "h2d_bytes": int(draws.nbytes), "d2h_bytes": int(shots.nbytes + ex.nbytes)}
+    b.free()
+    return out
+
+
+def run_serving(arrive_s: float = 1.5, drain_s: float = 60.0, seed: int = 5):
+    """Serving stream: Poisson arrivals (mean 200/s) of random-layer, QFT and
+    QAOA programs with 10..30 qubits, depth 5..40, shots 1..1e4, FP32 or FP64,
+    admitted by HBM bytes within 180 GB.  Arrivals for `arrive_s`, then the
+    queue drains for at most `drain_s`."""
+    from qvm_gb300.serve import Server, serving_workload
+    work = serving_workload(arrive_s, rate=200.0, seed=seed)
+    srv = Server(hbm_budget=180e9, workers=16)
+    subs = []
+    t0 = time.perf_counter()
+    for off, req in work:
+        now = time.perf_counter() - t0
+        if off > now:
+            time.sleep(off - now)
+        req.arrival = time.perf_counter()
+        subs.append((req, srv.submit(req)))
+    deadline = t0 + arrive_s + drain_s
+    done = []   # (completion instant, latency)
+    for req, f in subs:
+        try:
+            r = f.result(timeout=max(0.0, deadline - time.perf_counter()))
+            done.append((req.arrival + r.latency_s, r.latency_s, req.precision, req.n))
+        except Exception:
+            pass
+    srv.close_now()
+    lat = np.array([d[1] for d in done]) * 1e3
+    span = (max(d[0] for d in done) - t0) if done else float("nan")
+    small = np.array([d[1] for d in done if d[3] <= 24]) * 1e3
+    return {"requests": len(work), "completed": len(done), "arrival_rate": 200.0,
+            "qubits": "10..30", "budget_gb": 180, "arrivals_s": arrive_s,
+            "jobs_per_s": len(done) / span if done else 0.0,
+            "p50_ms": float(np.percentile(lat, 50)) if done else None,
+            "p99_ms": float(np.percentile(lat, 99)) if done else None,
+            "p50_ms_n_le_24": float(np.percentile(small, 50)) if len(small) else None,
+            "window_s": span}
+
+
 def run_reference(args):
     ws, rank, _ = dist()
     if rank != 0:
@@ -210,13 +276,15 @@ def main():
     s32 = CudaPureState(n, "fp32")
     stream = torch.cuda.ExternalStream(s32.stream())
     tuned = None
-    if args.fw == 0 or args.tile == 0:
-        # untimed: pick fusion width and tile width for this circuit on this GPU
+    if args.fw == 0 or args.tile == 0 or args.reg < 0:
+        # untimed: pick fusion width, tile width and register stages for this
+        # circuit on this GPU
         from qvm_gb300.autotune import DEFAULT_CANDIDATES, autotune
-        cands = [(fw, t) for fw, t in DEFAULT_CANDIDATES["fp32"]
-                 if (args.fw in (0, fw)) and (args.tile in (0, t))]
-        (args.fw, args.tile), table = autotune(prog, s32, "fp32", cands)
-        tuned = {f"fw{fw}_t{t}": round(ms, 2) for (fw, t), ms in sorted(table.items())}
+        cands = [(fw, t, r) for fw, t, r in DEFAULT_CANDIDATES["fp32"]
+                 if args.fw in (0, fw) and args.tile in (0, t) and args.reg in (-1, r)]
+        (args.fw, args.tile, args.reg), table = autotune(prog, s32, "fp32", cands)
+        tuned = {f"fw{fw}_t{t}_r{r}": round(ms, 2) for (fw, t, r), ms in sorted(table.items())}
+    prog.set_register_stages(bool(args.reg))
     stats = prog.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
 
     def step():
@@ -263,7 +331,8 @@ def main():
         "workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth {args.depth}, {G} gates, "
                     f"fused FP32 (fusion width {args.fw})",
         "passes": stats["passes"], "fused_blocks": stats["fused_blocks"],
-        "fusion_width": args.fw, "tile_qubits": args.tile, "autotune_ms": tuned,
+        "fusion_width": args.fw, "tile_qubits": args.tile, "register_stages": args.reg,
+        "autotune_ms": tuned,
         "state_bytes": state_bytes,
         "l2": "state (%.1f GiB) is larger than L2; no flush needed" % (state_bytes / 2 ** 30),
         "parallelism": f"replicas x{ws}"}
@@ -289,6 +358,7 @@ def main():
         t0 = time.perf_counter()
         p = Program()
         p.add_gates(gates)               # host gate matrices
+        p.set_register_stages(bool(args.reg))
         st = p.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
         s32.set_to_zero_state()
         p.run(s32, fused=True)           # plan upload + passes
@@ -329,6 +399,10 @@ def main():
                               "shots": int(args.shots),
                               "identical_shots": int((sh64 == sh32).sum())}
         s64.free()
+    if not args.no_batch and rank == 0:
+        result["batch_qaoa"] = run_qaoa_batch()
+    if not args.no_serve and rank == 0:
+        result["serving"] = run_serving()
     if not args.no_cpu and rank == 0:
         result["cpu_baseline"] = cpu_baseline(n, gates, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:

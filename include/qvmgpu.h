@@ -193,6 +193,12 @@ int qvmg_program_num_ops(qvmg_program p, int *nops);
  * tile, 0 = default).  *npasses receives the number of device passes. */
 int qvmg_program_plan(qvmg_program p, int nqubits, int precision, int mode,
                       int fusion_width, int tile_qubits, int *npasses);
+/* Planner options (QVMG_OPT_*), kept with the program and used by the next
+ * plan or run.  QVMG_OPT_REGISTER_STAGES: 1 = apply runs of 1-/2-qubit
+ * blocks to amplitudes held in registers inside a tile (FP32, 12/13-qubit
+ * tiles), 0 = every block through shared memory (default). */
+#define QVMG_OPT_REGISTER_STAGES 1
+int qvmg_program_set_option(qvmg_program p, int option, int value);
 /* Plan statistics: stats[0]=source ops, [1]=passes, [2]=tile passes,
  * [3]=fused blocks, [4]=diagonal passes, [5]=permutation passes,
  * [6]=algorithmic bytes moved per run (2 x state bytes x passes),

@@ -66,6 +66,7 @@ SIGNATURES = {
     "qvmg_program_num_ops": (_i, [_vp, _ip]),
     "qvmg_program_plan": (_i, [_vp, _i, _i, _i, _i, _i, _ip]),
     "qvmg_program_plan_stats": (_i, [_vp, _i64p, _i]),
+    "qvmg_program_set_option": (_i, [_vp, _i, _i]),
     "qvmg_program_plan_describe": (_i, [_vp, ctypes.c_char_p, _u64, _u64p]),
     "qvmg_program_run": (_i, [_vp, _vp, _i]),
     "qvmg_program_run_profiled": (_i, [_vp, _vp, _i, ctypes.POINTER(ctypes.c_float), _ip, _i, _ip]),

@@ -393,7 +393,12 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
   }
   QCHK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
   QCHK(cudaMalloc(&b->dbuf, host.size()), "cudaMalloc(batch tables)");
-  QCHK(cudaMemcpy(b->dbuf, host.data(), host.size(), cudaMemcpyHostToDevice), "cudaMemcpy");
+  // On the batch's own stream, then wait: a plain cudaMemcpy from pageable
+  // memory can return before its DMA lands, on a stream the batch's
+  // non-blocking stream does not wait for.
+  QCHK(cudaMemcpyAsync(b->dbuf, host.data(), host.size(), cudaMemcpyHostToDevice, b->stream),
+       "cudaMemcpyAsync(batch tables)");
+  QCHK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
   QCHK(cudaMalloc(&b->states, soff * sizeof(float2)), "cudaMalloc(batch states)");
   QCHK(cudaMalloc(&b->subs, uoff * sizeof(double)), "cudaMalloc(batch CDF)");
   QCHK(cudaMalloc(&b->expect, ninst * sizeof(double)), "cudaMalloc(expectations)");

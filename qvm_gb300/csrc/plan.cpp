@@ -293,6 +293,17 @@ static void plan_plain(const std::vector<Op> &ops, Plan &plan) {
   if (!run.empty()) emit_diag_passes(run, plan);
 }
 
+// Shared memory of a tile pass on the device: the tile, its row offsets
+// (padded to 16 bytes), op data and op / stage descriptors (tile.h).
+size_t tile_pass_smem_bytes(const Pass &p, int prec) {
+  size_t csz = prec == QVMG_FP64 ? 16 : 8;
+  size_t rows = (((size_t)1 << (p.t - p.L)) + 1) & ~(size_t)1;
+  size_t b = ((size_t)1 << p.t) * csz + rows * 8;
+  for (auto &o : p.tops) b += o.data.size() * csz + kTileOpDescBytes;
+  b += p.stages.size() * kTileStageDescBytes;
+  return (b + 15) & ~(size_t)15;
+}
+
 static void plan_fused(const std::vector<Op> &ops, int nq, int prec, int fw, int tile,
                        Plan &plan) {
   std::vector<Op> fused = fuse_ops(ops, fw);
@@ -346,56 +357,145 @@ static void plan_fused(const std::vector<Op> &ops, int nq, int prec, int fw, int
       emit_diag_passes(run, plan);
       continue;
     }
-    Pass p;
-    p.kind = Pass::TILE;
-    p.L = L;
-    // Fill the tile up to t qubits (unused tile bits cost nothing but keep
-    // the tile geometry fixed): take the lowest qubits not yet in the tile.
-    for (int q = L; q < nq && (int)E.size() < cap; ++q) E.insert(q);
-    p.E.assign(E.begin(), E.end());
-    p.t = L + (int)p.E.size();
-    auto local = [&](int q) {
-      if (q < L) return q;
-      return L + (int)(std::find(p.E.begin(), p.E.end(), q) - p.E.begin());
-    };
-    std::vector<const Op *> drun;
-    auto flush = [&]() {
-      if (drun.empty()) return;
-      std::vector<std::vector<int>> tq;
-      std::vector<std::vector<cd>> tables;
-      build_tables(drun, tq, tables);
-      for (size_t i = 0; i < tq.size(); ++i) {
+    // Build the pass; if its shared-memory image (tile + op data +
+    // descriptors) exceeds the per-CTA budget, hand the last ops back to the
+    // next pass (a suffix in program order, so every qubit keeps its order).
+    auto build_pass = [&](const std::vector<int> &members) {
+      Pass p;
+      p.kind = Pass::TILE;
+      p.L = L;
+      std::set<int> EE = E;
+      // Fill the tile up to t qubits (unused tile bits cost nothing but keep
+      // the tile geometry fixed): take the lowest qubits not yet in the tile.
+      for (int q = L; q < nq && (int)EE.size() < cap; ++q) EE.insert(q);
+      p.E.assign(EE.begin(), EE.end());
+      p.t = L + (int)p.E.size();
+      auto local = [&](int q) {
+        if (q < L) return q;
+        return L + (int)(std::find(p.E.begin(), p.E.end(), q) - p.E.begin());
+      };
+      std::vector<const Op *> drun;
+      auto flush = [&]() {
+        if (drun.empty()) return;
+        std::vector<std::vector<int>> tq;
+        std::vector<std::vector<cd>> tables;
+        build_tables(drun, tq, tables);
+        for (size_t i = 0; i < tq.size(); ++i) {
+          TileOpHost top;
+          top.kind = OP_DIAG;
+          top.pos = tq[i];
+          top.data = tables[i];
+          p.tops.push_back(std::move(top));
+        }
+        drun.clear();
+      };
+      for (int u : members) {
+        const Op &op = units[u];
+        if (op.kind == OP_DIAG) {
+          drun.push_back(&op);
+          continue;
+        }
+        flush();
         TileOpHost top;
-        top.kind = OP_DIAG;
-        top.pos = tq[i];
-        top.data = tables[i];
+        top.kind = op.kind;
+        for (int q : op.q) top.pos.push_back(local(q));
+        if (op.kind == OP_DENSE) top.data = op.m;
+        else top.perm = op.perm;
         p.tops.push_back(std::move(top));
       }
-      drun.clear();
-    };
-    for (int u : in_pass) {
-      const Op &op = units[u];
-      if (op.kind == OP_DIAG) {
-        drun.push_back(&op);
-        continue;
-      }
       flush();
-      TileOpHost top;
-      top.kind = op.kind;
-      for (int q : op.q) top.pos.push_back(local(q));
-      if (op.kind == OP_DENSE) top.data = op.m;
-      else top.perm = op.perm;
-      p.tops.push_back(std::move(top));
+      build_stages(p, prec, plan.reg_stages);
+      return p;
+    };
+    Pass p = build_pass(in_pass);
+    while (tile_pass_smem_bytes(p, prec) > kTileSmemBudget && in_pass.size() > 1) {
+      remaining.insert(std::lower_bound(remaining.begin(), remaining.end(), in_pass.back()),
+                       in_pass.back());
+      in_pass.pop_back();
+      p = build_pass(in_pass);
     }
-    flush();
     plan.passes.push_back(std::move(p));
     plan.n_tile++;
   }
 }
 
+int tile_register_bits(int prec, int t) {
+  if (prec != QVMG_FP32) return 0;
+  int r = t - 8;  // 256 threads
+  return (r == 4 || r == 5) ? r : 0;
+}
+
+// Swap the matrix index bits of a 2-qubit op (so its qubit order flips).
+static std::vector<cd> swap_2q(const std::vector<cd> &m) {
+  auto sw = [](int i) { return ((i & 1) << 1) | ((i >> 1) & 1); };
+  std::vector<cd> out(16);
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) out[(size_t)sw(r) * 4 + sw(c)] = m[(size_t)r * 4 + c];
+  return out;
+}
+
+void build_stages(Pass &p, int prec, bool reg_stages) {
+  p.stages.clear();
+  p.R = reg_stages ? tile_register_bits(prec, p.t) : 0;
+  const int n = (int)p.tops.size();
+  if (p.R == 0) {
+    for (int i = 0; i < n; ++i) {
+      TileStage s;
+      s.first = i;
+      s.count = 1;
+      p.stages.push_back(s);
+    }
+    return;
+  }
+  auto reg_ok = [&](const TileOpHost &o) { return o.kind == OP_DENSE && o.pos.size() <= 2; };
+  int i = 0;
+  while (i < n) {
+    if (!reg_ok(p.tops[i])) {
+      TileStage s;
+      s.first = i;
+      s.count = 1;
+      p.stages.push_back(s);
+      ++i;
+      continue;
+    }
+    // the longest run of register ops whose tile bits fit R slots
+    std::set<int> bits;
+    int j = i;
+    while (j < n && reg_ok(p.tops[j])) {
+      std::set<int> u = bits;
+      u.insert(p.tops[j].pos.begin(), p.tops[j].pos.end());
+      if ((int)u.size() > p.R) break;
+      bits.swap(u);
+      ++j;
+    }
+    TileStage s;
+    s.reg = true;
+    s.first = i;
+    s.count = j - i;
+    // pad the slots with the highest free tile bits, so that the thread bits
+    // (the warp lanes) keep the low bits: consecutive lanes then touch
+    // neighbouring shared-memory words
+    for (int b = p.t - 1; b >= 0 && (int)bits.size() < p.R; --b) bits.insert(b);
+    s.slots.assign(bits.begin(), bits.end());
+    for (int b = 0; b < p.t; ++b)
+      if (!bits.count(b)) s.tpos.push_back(b);
+    // canonical qubit order: ascending slots (matrix index bit 0 = lower slot)
+    for (int o = i; o < j; ++o) {
+      TileOpHost &op = p.tops[o];
+      if (op.pos.size() == 2 && op.pos[0] > op.pos[1]) {
+        std::swap(op.pos[0], op.pos[1]);
+        op.data = swap_2q(op.data);
+      }
+    }
+    p.stages.push_back(s);
+    i = j;
+  }
+}
+
 void make_plan(const std::vector<Op> &ops, int nq, int prec, int mode, int fw, int tile,
-               Plan &plan) {
+               Plan &plan, bool reg_stages) {
   plan = Plan();
+  plan.reg_stages = reg_stages;
   plan.nq = nq;
   plan.prec = prec;
   plan.mode = mode;

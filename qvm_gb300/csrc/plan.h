@@ -30,6 +30,17 @@ struct TileOpHost {
   std::vector<int64_t> perm; // perm moves
 };
 
+// A stage of a tile pass: either a run of 1- and 2-qubit dense ops applied to
+// amplitudes held in registers (each thread owns 2^R of them: the tile bits
+// `slots`, R of them, ascending; the other tile bits index the thread), or a
+// single op applied in shared memory.
+struct TileStage {
+  bool reg = false;
+  int first = 0, count = 0;  // ops [first, first+count) of the pass
+  std::vector<int> slots;    // register stage: tile bits of register slots 0..R-1
+  std::vector<int> tpos;     // register stage: tile bits of thread-index bits, ascending
+};
+
 struct Pass {
   enum Kind { DENSE = 0, DIAG = 1, PERM = 2, TILE = 3 } kind;
   // DENSE / PERM: a single op (global qubits)
@@ -41,10 +52,28 @@ struct Pass {
   int t = 0, L = 0;
   std::vector<int> E;  // global positions of tile bits L..t-1, ascending
   std::vector<TileOpHost> tops;
+  int R = 0;           // register bits of the register stages (0: none)
+  std::vector<TileStage> stages;
 };
+
+// Device descriptor sizes of tile ops and stages (tile.h), and the shared
+// memory one tile pass may use (227 KiB per CTA on sm_103a).
+constexpr size_t kTileOpDescBytes = 128;
+constexpr size_t kTileStageDescBytes = 80;
+constexpr size_t kTileSmemBudget = 227 * 1024;
+size_t tile_pass_smem_bytes(const Pass &p, int prec);
+
+// Register bits per thread for a tile of t qubits run by 256 threads:
+// FP32 tiles of 12 or 13 qubits hold 16 or 32 amplitudes per thread; other
+// tiles (and FP64, whose 16-byte amplitudes would not fit) use shared memory.
+int tile_register_bits(int prec, int t);
+// Group a tile pass's ops into stages (register runs and shared-memory ops);
+// canonicalises register ops so their slots ascend.
+void build_stages(Pass &p, int prec, bool reg_stages);
 
 struct Plan {
   int nq = -1, prec = -1, mode = -1, fw = -1, tile = -1;
+  bool reg_stages = false;
   std::vector<Pass> passes;
   int64_t n_src = 0, n_blocks = 0, n_tile = 0, n_diag = 0, n_perm = 0, n_dense = 0;
 };
@@ -53,7 +82,7 @@ struct Plan {
 std::vector<Op> fuse_ops(const std::vector<Op> &ops, int fw);
 // Build a plan for a state of nq qubits.
 void make_plan(const std::vector<Op> &ops, int nq, int prec, int mode, int fw, int tile,
-               Plan &plan);
+               Plan &plan, bool reg_stages = false);
 // Default tile width (qubits held per tile) for a precision.
 int default_tile_qubits(int prec);
 int tile_low_bits(int prec);

@@ -23,6 +23,10 @@
 
 namespace qvmg {
 
+static_assert(sizeof(TileOpDev) == kTileOpDescBytes, "planner op descriptor size");
+static_assert(sizeof(TileStageDev) == kTileStageDescBytes, "planner stage descriptor size");
+static_assert(kTileMaxSmem == (int)kTileSmemBudget, "planner shared-memory budget");
+
 // Device image of one plan for one precision.
 struct DevicePlan {
   Plan plan;
@@ -41,11 +45,12 @@ struct DevicePlan {
 struct qvmg_program_s {
   std::vector<qvmg::Op> ops;
   std::mutex mu;
-  // key: (nq, prec, mode, fw, tile)
-  std::map<std::tuple<int, int, int, int, int>, std::unique_ptr<qvmg::DevicePlan>> plans;
+  // key: (nq, prec, mode, fw, tile, register stages)
+  std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<qvmg::DevicePlan>> plans;
   qvmg::Plan last_plan;  // most recent host-only plan (for statistics)
   int default_fw = 2;
   int default_tile = 0;
+  int reg_stages = 0;
 };
 
 namespace qvmg {
@@ -66,8 +71,8 @@ static void align16(std::vector<unsigned char> &bytes) {
 }
 
 static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw, int tile,
-                             DevicePlan &dp) {
-  make_plan(p->ops, nq, prec, mode, fw, tile, dp.plan);
+                             DevicePlan &dp, cudaStream_t stream) {
+  make_plan(p->ops, nq, prec, mode, fw, tile, dp.plan, p->reg_stages != 0);
   std::vector<unsigned char> bytes;
   const size_t csz = prec == QVMG_FP64 ? 16 : 8;
   dp.pass_off.assign(dp.plan.passes.size(), 0);
@@ -124,6 +129,35 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
       }
       ta.ndata = ndata;
       if (ta.kmax == 0) ta.kmax = 1;  // diagonal-only tile
+      // stages; register-stage ops carry their register slots
+      ta.R = ps.R;
+      std::vector<TileStageDev> sdev(ps.stages.size());
+      for (size_t si = 0; si < ps.stages.size(); ++si) {
+        const TileStage &st = ps.stages[si];
+        TileStageDev &sd = sdev[si];
+        std::memset(&sd, 0, sizeof(sd));
+        sd.reg = st.reg ? 1 : 0;
+        sd.first = st.first;
+        sd.count = st.count;
+        if (st.reg) {
+          if ((int)st.slots.size() != ps.R || (int)st.tpos.size() != ps.t - ps.R ||
+              st.tpos.size() > 10)
+            return fail(QVMG_E_UNSUPPORTED, "register stage geometry out of range");
+          for (size_t k = 0; k < st.slots.size(); ++k) sd.slots[k] = st.slots[k];
+          for (size_t k = 0; k < st.tpos.size(); ++k) sd.tpos[k] = st.tpos[k];
+          for (int o = st.first; o < st.first + st.count; ++o) {
+            TileOpDev &d = descs[o];
+            auto slot_of = [&](int b) {
+              return (int)(std::find(st.slots.begin(), st.slots.end(), b) - st.slots.begin());
+            };
+            d.slot0 = slot_of(d.pos[0]);
+            d.slot1 = d.k > 1 ? slot_of(d.pos[1]) : 0;
+            if (d.slot0 >= ps.R || (d.k > 1 && (d.slot1 >= ps.R || d.slot1 <= d.slot0)))
+              return fail(QVMG_E_UNSUPPORTED, "register op outside its stage's slots");
+          }
+        }
+      }
+      ta.nstages = (int)sdev.size();
       size_t data_off = bytes.size();
       if (prec == QVMG_FP64) put_complex<double>(bytes, data);
       else put_complex<float>(bytes, data);
@@ -131,23 +165,35 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
       size_t ops_off = bytes.size();
       bytes.resize(ops_off + descs.size() * sizeof(TileOpDev));
       std::memcpy(bytes.data() + ops_off, descs.data(), descs.size() * sizeof(TileOpDev));
+      align16(bytes);
+      size_t stages_off = bytes.size();
+      bytes.resize(stages_off + sdev.size() * sizeof(TileStageDev));
+      std::memcpy(bytes.data() + stages_off, sdev.data(), sdev.size() * sizeof(TileStageDev));
       // pointers are patched after upload
       ta.data = (const void *)data_off;
       ta.ops = (const void *)ops_off;
-      if (tile_smem_bytes(prec, ta.t, ta.L, ta.ndata, ta.nops) > (size_t)kTileMaxSmem)
+      ta.stages = (const void *)stages_off;
+      if (tile_smem_bytes(prec, ta.t, ta.L, ta.ndata, ta.nops, ta.nstages) > (size_t)kTileMaxSmem)
         return fail(QVMG_E_UNSUPPORTED, "tile pass data exceeds shared memory");
     }
   }
   (void)csz;
   if (!bytes.empty()) {
     QVMG_CUDA(cudaMalloc(&dp.buf, bytes.size()));
-    QVMG_CUDA(cudaMemcpy(dp.buf, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
+    // Upload on the state's stream and wait for it: a plain cudaMemcpy from
+    // pageable memory may return before its DMA lands, and it is ordered on
+    // the legacy default stream, which the state's non-blocking stream does
+    // not wait for -- a kernel could read the descriptors before they arrive.
+    QVMG_CUDA(cudaMemcpyAsync(dp.buf, bytes.data(), bytes.size(), cudaMemcpyHostToDevice,
+                              stream));
+    QVMG_CUDA(cudaStreamSynchronize(stream));
   }
   for (size_t i = 0; i < dp.plan.passes.size(); ++i) {
     if (dp.plan.passes[i].kind != Pass::TILE) continue;
     TileArgs &ta = dp.tile_args[i];
     ta.data = (const unsigned char *)dp.buf + (size_t)ta.data;
     ta.ops = (const unsigned char *)dp.buf + (size_t)ta.ops;
+    ta.stages = (const unsigned char *)dp.buf + (size_t)ta.stages;
   }
   return QVMG_OK;
 }
@@ -262,6 +308,16 @@ static std::string describe_plan(const Plan &pl) {
       s += "{\"kind\":\"tile\",\"t\":" + std::to_string(ps.t) + ",\"L\":" + std::to_string(ps.L) +
            ",\"E\":";
       ints(ps.E);
+      s += ",\"R\":" + std::to_string(ps.R) + ",\"stages\":[";
+      for (size_t si = 0; si < ps.stages.size(); ++si) {
+        const TileStage &st = ps.stages[si];
+        if (si) s += ",";
+        s += "{\"reg\":" + std::to_string(st.reg ? 1 : 0) + ",\"first\":" +
+             std::to_string(st.first) + ",\"count\":" + std::to_string(st.count) + ",\"slots\":";
+        ints(st.slots);
+        s += "}";
+      }
+      s += "]";
       s += ",\"ops\":[";
       for (size_t o = 0; o < ps.tops.size(); ++o) {
         const TileOpHost &th = ps.tops[o];
@@ -385,11 +441,23 @@ int qvmg_program_plan(qvmg_program p, int nqubits, int precision, int mode, int 
   std::lock_guard<std::mutex> g(p->mu);
   if (program_max_qubit(p) > nqubits)
     return fail(QVMG_E_INVALID, "program uses a qubit beyond the state's qubit count");
-  make_plan(p->ops, nqubits, precision, mode, fusion_width, tile_qubits, p->last_plan);
+  make_plan(p->ops, nqubits, precision, mode, fusion_width, tile_qubits, p->last_plan,
+            p->reg_stages != 0);
   p->default_fw = fusion_width;
   p->default_tile = tile_qubits;
   if (npasses) *npasses = (int)p->last_plan.passes.size();
   return QVMG_OK;
+}
+
+int qvmg_program_set_option(qvmg_program p, int option, int value) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  std::lock_guard<std::mutex> g(p->mu);
+  if (option == QVMG_OPT_REGISTER_STAGES) {
+    if (value != 0 && value != 1) return fail(QVMG_E_INVALID, "register stages option is 0 or 1");
+    p->reg_stages = value;
+    return QVMG_OK;
+  }
+  return fail(QVMG_E_INVALID, "unknown program option " + std::to_string(option));
 }
 
 int qvmg_program_plan_stats(qvmg_program p, int64_t *stats, int nstats) {
@@ -433,11 +501,11 @@ static int device_plan_for(qvmg_state s, qvmg_program p, int mode, DevicePlan **
     return fail(QVMG_E_INVALID, "program uses a qubit beyond the state's qubit count");
   int fw = mode == QVMG_RUN_FUSED ? p->default_fw : 1;
   int tile = mode == QVMG_RUN_FUSED ? p->default_tile : 0;
-  auto key = std::make_tuple(s->nq, s->prec, mode, fw, tile);
+  auto key = std::make_tuple(s->nq, s->prec, mode, fw, tile, p->reg_stages);
   auto it = p->plans.find(key);
   if (it == p->plans.end()) {
     auto dp = std::make_unique<DevicePlan>();
-    if ((rc = build_device_plan(p, s->nq, s->prec, mode, fw, tile, *dp))) return rc;
+    if ((rc = build_device_plan(p, s->nq, s->prec, mode, fw, tile, *dp, s->stream))) return rc;
     it = p->plans.emplace(key, std::move(dp)).first;
   }
   *out = it->second.get();

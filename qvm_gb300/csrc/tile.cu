@@ -2,15 +2,26 @@
 //
 // One pass applies a sequence of fused gate blocks to the whole state with a
 // single read and a single write of every amplitude.  The state is cut into
-// 2^(n-t) tiles of 2^t amplitudes: tile-local bits 0..L-1 are global qubits
-// 0..L-1 (a 256-byte contiguous row), bits L..t-1 are the pass's chosen
-// global qubits E[0..].  A CTA loads a tile row by row with 16-byte vector
-// loads into shared memory, applies every op of the pass there (dense k<=5
-// blocks gathered into registers, permutations as register moves, diagonal
-// phase tables indexed by the global address), then writes the rows back.
+// 2^(n-t) tiles of 2^t amplitudes: tile bits 0..L-1 are global qubits 0..L-1
+// (a 256-byte contiguous row), bits L..t-1 are the pass's chosen global
+// qubits E[0..].  A CTA streams tiles into shared memory with 16-byte
+// asynchronous copies (cp.async), applies every op of the pass there, and
+// writes the tile back.  The ops run in stages:
+//  - register stages: each of the 256 threads owns 2^R amplitudes of the
+//    tile (R tile bits, the stage's "slots"; the other 8 bits index the
+//    thread).  A run of 1- and 2-qubit dense blocks whose bits fit the slots
+//    is applied entirely in registers -- fully unrolled complex FMAs with the
+//    block matrix held in registers, no shared-memory traffic and no address
+//    arithmetic per op;
+//  - shared-memory stages: diagonal phase tables (indexed by the global
+//    address), permutations, and dense blocks of 3..5 qubits, one group of
+//    2^k amplitudes per thread.
+// Shared memory is XOR-swizzled (bits 1..3 of a tile index are XORed with
+// bits 4..12 folded) so that the lanes of a warp spread over the banks in
+// both the row-contiguous copies and the register-stage gathers.
 // This is the GB300 form of the reference's per-gate complement iteration
 // (src/wavefunction.lisp:155-306, src/compile-gate.lisp:23-209): the same
-// gather -> matvec -> scatter, but over shared memory for many gates at once.
+// gather -> matvec -> scatter, for many gates per HBM round trip.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,10 +44,17 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// Bank swizzle: linear in the index bits (XOR), keeps bit 0 (16-byte pairs).
+__host__ __device__ __forceinline__ unsigned swz(unsigned j) {
+  return j ^ ((((j >> 4) ^ (j >> 7) ^ (j >> 10)) & 7u) << 1);
+}
+
 __device__ __forceinline__ unsigned inject0u(unsigned x, int q) {
   unsigned lo = x & ((1u << q) - 1u);
   return ((x >> q) << (q + 1)) | lo;
 }
+
+// ---- shared-memory ops -----------------------------------------------------------
 
 template <typename T, int K>
 __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const TileOpDev &op,
@@ -46,7 +64,6 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
   int sp[K];
 #pragma unroll
   for (int i = 0; i < K; ++i) sp[i] = op.pos[i];
-  // insertion sort (K <= 5)
 #pragma unroll
   for (int i = 1; i < K; ++i)
 #pragma unroll
@@ -66,40 +83,19 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
     off[c] = o;
   }
   const unsigned ngroups = 1u << (t - K);
-  if (K <= 2) {
-    C m[D * D];
+  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
+    unsigned b = g;
 #pragma unroll
-    for (int i = 0; i < D * D; ++i) m[i] = mat[i];
-    for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
-      unsigned b = g;
+    for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
+    C v[D];
 #pragma unroll
-      for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
-      C v[D];
+    for (int c = 0; c < D; ++c) v[c] = tile[swz(b | off[c])];
 #pragma unroll
-      for (int c = 0; c < D; ++c) v[c] = tile[b + off[c]];
+    for (int r = 0; r < D; ++r) {
+      C acc = CT<T>::make(0, 0);
 #pragma unroll
-      for (int r = 0; r < D; ++r) {
-        C acc = CT<T>::make(0, 0);
-#pragma unroll
-        for (int c = 0; c < D; ++c) cmac(acc, m[r * D + c], v[c]);
-        tile[b + off[r]] = acc;
-      }
-    }
-  } else {
-    for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
-      unsigned b = g;
-#pragma unroll
-      for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
-      C v[D];
-#pragma unroll
-      for (int c = 0; c < D; ++c) v[c] = tile[b + off[c]];
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        C acc = CT<T>::make(0, 0);
-#pragma unroll
-        for (int c = 0; c < D; ++c) cmac(acc, mat[r * D + c], v[c]);
-        tile[b + off[r]] = acc;
-      }
+      for (int c = 0; c < D; ++c) cmac(acc, mat[r * D + c], v[c]);
+      tile[swz(b | off[r])] = acc;
     }
   }
 }
@@ -138,10 +134,10 @@ __device__ __forceinline__ void tile_perm(typename CT<T>::C *tile, int t, const 
     C v[D];
 #pragma unroll
     for (int j = 0; j < D; ++j)
-      if (j < nm) v[j] = tile[b + off[op.src[j]]];
+      if (j < nm) v[j] = tile[swz(b | off[op.src[j]])];
 #pragma unroll
     for (int j = 0; j < D; ++j)
-      if (j < nm) tile[b + off[op.dst[j]]] = v[j];
+      if (j < nm) tile[swz(b | off[op.dst[j]])] = v[j];
   }
 }
 
@@ -158,14 +154,144 @@ __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
     int idx = 0;
     for (int i = 0; i < k; ++i) idx |= (int)((g >> op.pos[i]) & 1ull) << i;
     C ph = table[idx];
-    if (ph.x != (T)1 || ph.y != (T)0) tile[j] = cmul(tile[j], ph);
+    if (ph.x != (T)1 || ph.y != (T)0) {
+      const unsigned p = swz(j);
+      tile[p] = cmul(tile[p], ph);
+    }
   }
 }
 
-// KMAX: widest op of the pass; narrower instantiations keep the register
-// arrays of the wide cases out of the kernel (no spills for k <= 2).
+// ---- register stages (FP32) ---------------------------------------------------------
+
+// 1-qubit block on register slot S of 2^R registers.
+template <int R, int S>
+__device__ __forceinline__ void reg_op1(float2 *v, const float2 *m) {
+  const float2 m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+#pragma unroll
+  for (int g = 0; g < (1 << (R - 1)); ++g) {
+    const int b = ((g >> S) << (S + 1)) | (g & ((1 << S) - 1));
+    const float2 a0 = v[b], a1 = v[b | (1 << S)];
+    float2 r0 = cmul(m00, a0), r1 = cmul(m10, a0);
+    cmac(r0, m01, a1);
+    cmac(r1, m11, a1);
+    v[b] = r0;
+    v[b | (1 << S)] = r1;
+  }
+}
+
+// 2-qubit block on register slots S0 < S1 (matrix index bit 0 <-> S0).
+template <int R, int S0, int S1>
+__device__ __forceinline__ void reg_op2(float2 *v, const float2 *m) {
+  float2 mm[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) mm[i] = m[i];
+#pragma unroll
+  for (int g = 0; g < (1 << (R - 2)); ++g) {
+    int b = ((g >> S0) << (S0 + 1)) | (g & ((1 << S0) - 1));
+    b = ((b >> S1) << (S1 + 1)) | (b & ((1 << S1) - 1));
+    const int i1 = b | (1 << S0), i2 = b | (1 << S1), i3 = b | (1 << S0) | (1 << S1);
+    const float2 a0 = v[b], a1 = v[i1], a2 = v[i2], a3 = v[i3];
+    float2 r[4];
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+      float2 acc = cmul(mm[row * 4], a0);
+      cmac(acc, mm[row * 4 + 1], a1);
+      cmac(acc, mm[row * 4 + 2], a2);
+      cmac(acc, mm[row * 4 + 3], a3);
+      r[row] = acc;
+    }
+    v[b] = r[0];
+    v[i1] = r[1];
+    v[i2] = r[2];
+    v[i3] = r[3];
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void reg_apply(float2 *v, const TileOpDev &op, const float2 *m) {
+  if (op.k == 1) {
+    switch (op.slot0) {
+      case 0: reg_op1<R, 0>(v, m); break;
+      case 1: reg_op1<R, 1>(v, m); break;
+      case 2: reg_op1<R, 2>(v, m); break;
+      case 3: reg_op1<R, 3>(v, m); break;
+      case 4: if constexpr (R > 4) reg_op1<R, 4>(v, m); break;
+    }
+    return;
+  }
+  switch (op.slot0 * 8 + op.slot1) {
+    case 0 * 8 + 1: reg_op2<R, 0, 1>(v, m); break;
+    case 0 * 8 + 2: reg_op2<R, 0, 2>(v, m); break;
+    case 0 * 8 + 3: reg_op2<R, 0, 3>(v, m); break;
+    case 1 * 8 + 2: reg_op2<R, 1, 2>(v, m); break;
+    case 1 * 8 + 3: reg_op2<R, 1, 3>(v, m); break;
+    case 2 * 8 + 3: reg_op2<R, 2, 3>(v, m); break;
+    case 0 * 8 + 4: if constexpr (R > 4) reg_op2<R, 0, 4>(v, m); break;
+    case 1 * 8 + 4: if constexpr (R > 4) reg_op2<R, 1, 4>(v, m); break;
+    case 2 * 8 + 4: if constexpr (R > 4) reg_op2<R, 2, 4>(v, m); break;
+    case 3 * 8 + 4: if constexpr (R > 4) reg_op2<R, 3, 4>(v, m); break;
+  }
+}
+
+// A register stage: gather this thread's 2^R amplitudes, run the ops, scatter.
+// The swizzle is linear, so swz(x | r) = swz(x) ^ swz(r) for disjoint bits.
+template <int R>
+__device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDev &st,
+                                          const TileOpDev *ops, const float2 *data) {
+  unsigned xb = 0;
+  for (int i = 0; i < t - R; ++i)
+    if ((threadIdx.x >> i) & 1u) xb |= 1u << st.tpos[i];
+  const unsigned px = swz(xb);
+  unsigned lo[4], hi[1 << (R - 2)];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    lo[r] = swz(((r & 1) ? 1u << st.slots[0] : 0u) | ((r & 2) ? 1u << st.slots[1] : 0u)) ^ px;
+#pragma unroll
+  for (int h = 0; h < (1 << (R - 2)); ++h) {
+    unsigned o = 0;
+#pragma unroll
+    for (int i = 0; i < R - 2; ++i)
+      if ((h >> i) & 1) o |= 1u << st.slots[2 + i];
+    hi[h] = swz(o);
+  }
+  float2 v[1 << R];
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) v[r] = tile[lo[r & 3] ^ hi[r >> 2]];
+  for (int o = st.first; o < st.first + st.count; ++o) reg_apply<R>(v, ops[o], data + ops[o].data);
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) tile[lo[r & 3] ^ hi[r >> 2]] = v[r];
+}
+
 template <typename T, int KMAX>
-__global__ void __launch_bounds__(kTileThreads, KMAX <= 2 ? 3 : 1)
+__device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
+                                        const unsigned long long *rowoff, const TileOpDev &op,
+                                        const typename CT<T>::C *md) {
+  if (op.kind == 0) {
+    switch (op.k) {
+      case 1: tile_dense<T, 1>(tile, t, op, md); break;
+      case 2: tile_dense<T, 2>(tile, t, op, md); break;
+      case 3: if constexpr (KMAX >= 3) tile_dense<T, 3>(tile, t, op, md); break;
+      case 4: if constexpr (KMAX >= 4) tile_dense<T, 4>(tile, t, op, md); break;
+      case 5: if constexpr (KMAX >= 5) tile_dense<T, 5>(tile, t, op, md); break;
+    }
+  } else if (op.kind == 2) {
+    switch (op.k) {
+      case 1: tile_perm<T, 1>(tile, t, op); break;
+      case 2: tile_perm<T, 2>(tile, t, op); break;
+      case 3: if constexpr (KMAX >= 3) tile_perm<T, 3>(tile, t, op); break;
+      case 4: if constexpr (KMAX >= 4) tile_perm<T, 4>(tile, t, op); break;
+      case 5: if constexpr (KMAX >= 5) tile_perm<T, 5>(tile, t, op); break;
+    }
+  } else {
+    tile_diag<T>(tile, t, L, rowoff, op, md);
+  }
+}
+
+// KMAX: widest op of the pass; RB: register bits of the register stages
+// (0: every stage runs in shared memory).  Narrow instantiations keep the
+// register arrays of wide cases out of the kernel.
+template <typename T, int KMAX, int RB>
+__global__ void __launch_bounds__(kTileThreads, RB == 5 ? 2 : (KMAX <= 2 ? 3 : 1))
     k_tile(typename CT<T>::C *__restrict__ a, const __grid_constant__ TileArgs p) {
   using C = typename CT<T>::C;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -176,6 +302,7 @@ __global__ void __launch_bounds__(kTileThreads, KMAX <= 2 ? 3 : 1)
   // row offsets padded to 16 bytes so that double2 op data stays aligned
   C *data = reinterpret_cast<C *>(rowoff + ((nrows + 1u) & ~1u));
   TileOpDev *ops = reinterpret_cast<TileOpDev *>(data + p.ndata);
+  TileStageDev *stages = reinterpret_cast<TileStageDev *>(ops + p.nops);
   {
     const C *gd = reinterpret_cast<const C *>(p.data);
     for (int i = threadIdx.x; i < p.ndata; i += blockDim.x) data[i] = gd[i];
@@ -183,6 +310,10 @@ __global__ void __launch_bounds__(kTileThreads, KMAX <= 2 ? 3 : 1)
     int *ss = reinterpret_cast<int *>(ops);
     const int words = p.nops * (int)(sizeof(TileOpDev) / 4);
     for (int i = threadIdx.x; i < words; i += blockDim.x) ss[i] = gs[i];
+    const int *gt = reinterpret_cast<const int *>(p.stages);
+    int *st = reinterpret_cast<int *>(stages);
+    const int swords = p.nstages * (int)(sizeof(TileStageDev) / 4);
+    for (int i = threadIdx.x; i < swords; i += blockDim.x) st[i] = gt[i];
   }
   constexpr int per16 = 16 / sizeof(C);  // amplitudes per 16-byte chunk
   const unsigned nchunks = (1u << t) / per16;
@@ -204,85 +335,81 @@ __global__ void __launch_bounds__(kTileThreads, KMAX <= 2 ? 3 : 1)
     __syncthreads();
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
-      const int4 *src = reinterpret_cast<const int4 *>(a + rowoff[el >> L] + (el & rowmask));
-      cp_async16(reinterpret_cast<int4 *>(tile) + ch, src);
+      const C *src = a + rowoff[el >> L] + (el & rowmask);
+      cp_async16(tile + swz(el), src);
     }
     cp_async_wait_all();
     __syncthreads();
-    for (int o = 0; o < p.nops; ++o) {
-      const TileOpDev &op = ops[o];
-      const C *md = data + op.data;
-      if (op.kind == 0) {
-        switch (op.k) {
-          case 1: tile_dense<T, 1>(tile, t, op, md); break;
-          case 2: tile_dense<T, 2>(tile, t, op, md); break;
-          case 3: if constexpr (KMAX >= 3) tile_dense<T, 3>(tile, t, op, md); break;
-          case 4: if constexpr (KMAX >= 4) tile_dense<T, 4>(tile, t, op, md); break;
-          case 5: if constexpr (KMAX >= 5) tile_dense<T, 5>(tile, t, op, md); break;
+    for (int s = 0; s < p.nstages; ++s) {
+      const TileStageDev &st = stages[s];
+      if constexpr (RB > 0) {
+        if (st.reg) {
+          reg_stage<RB>(reinterpret_cast<float2 *>(tile), t, st, ops,
+                        reinterpret_cast<const float2 *>(data));
+          __syncthreads();
+          continue;
         }
-      } else if (op.kind == 2) {
-        switch (op.k) {
-          case 1: tile_perm<T, 1>(tile, t, op); break;
-          case 2: tile_perm<T, 2>(tile, t, op); break;
-          case 3: if constexpr (KMAX >= 3) tile_perm<T, 3>(tile, t, op); break;
-          case 4: if constexpr (KMAX >= 4) tile_perm<T, 4>(tile, t, op); break;
-          case 5: if constexpr (KMAX >= 5) tile_perm<T, 5>(tile, t, op); break;
-        }
-      } else {
-        tile_diag<T>(tile, t, L, rowoff, op, md);
       }
+      const TileOpDev &op = ops[st.first];
+      smem_op<T, KMAX>(tile, t, L, rowoff, op, data + op.data);
       __syncthreads();
     }
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
       int4 *dst = reinterpret_cast<int4 *>(a + rowoff[el >> L] + (el & rowmask));
-      __stcs(dst, reinterpret_cast<const int4 *>(tile)[ch]);
+      __stcs(dst, *reinterpret_cast<const int4 *>(tile + swz(el)));
     }
   }
 }
 
-size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops) {
+size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages) {
   size_t csz = prec == QVMG_FP64 ? 16 : 8;
   size_t rows = ((size_t)1 << (t - L)) + 1 & ~(size_t)1;  // padded to 16 bytes
   size_t b = ((size_t)1 << t) * csz + rows * 8 + (size_t)ndata * csz +
-             (size_t)nops * sizeof(TileOpDev);
+             (size_t)nops * sizeof(TileOpDev) + (size_t)nstages * sizeof(TileStageDev);
   return (b + 15) & ~(size_t)15;
 }
 
-template <typename T, int KMAX>
+template <typename T, int KMAX, int RB>
 static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
   static bool attr = false;  // per instantiation
   if (!attr) {
-    QVMG_CUDA(cudaFuncSetAttribute(k_tile<T, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   kTileMaxSmem));
+    QVMG_CUDA(cudaFuncSetAttribute(k_tile<T, KMAX, RB>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kTileMaxSmem));
     attr = true;
   }
   // Persistent grid: as many CTAs as fit on every SM at once (registers and
   // shared memory), each looping over tiles.
   int per_sm = 0;
-  QVMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<T, KMAX>, kTileThreads,
-                                                          smem));
+  QVMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<T, KMAX, RB>,
+                                                          kTileThreads, smem));
   if (per_sm < 1) return fail(QVMG_E_UNSUPPORTED, "tile pass does not fit on an SM");
   uint64_t grid = std::min<uint64_t>(args.ntiles, (uint64_t)sm_count() * per_sm);
-  k_tile<T, KMAX><<<(unsigned)grid, kTileThreads, smem, s->stream>>>(
+  k_tile<T, KMAX, RB><<<(unsigned)grid, kTileThreads, smem, s->stream>>>(
       (typename CT<T>::C *)s->amps, args);
   QVMG_CHECK_LAUNCH("k_tile");
   return QVMG_OK;
 }
 
-template <typename T>
-static int tile_launch(qvmg_state s, const TileArgs &args, size_t smem) {
-  if (args.kmax <= 2) return tile_launch_k<T, 2>(s, args, smem);
-  if (args.kmax <= 3) return tile_launch_k<T, 3>(s, args, smem);
-  return tile_launch_k<T, 5>(s, args, smem);
+template <typename T, int RB>
+static int tile_launch_r(qvmg_state s, const TileArgs &args, size_t smem) {
+  if (args.kmax <= 2) return tile_launch_k<T, 2, RB>(s, args, smem);
+  if (args.kmax <= 3) return tile_launch_k<T, 3, RB>(s, args, smem);
+  return tile_launch_k<T, 5, RB>(s, args, smem);
 }
 
 int launch_tile(qvmg_state s, const TileArgs &args) {
-  size_t smem = tile_smem_bytes(s->prec, args.t, args.L, args.ndata, args.nops);
+  size_t smem = tile_smem_bytes(s->prec, args.t, args.L, args.ndata, args.nops, args.nstages);
   if (smem > (size_t)kTileMaxSmem) return fail(QVMG_E_UNSUPPORTED, "tile pass exceeds shared memory");
   if (args.kmax < 1 || args.kmax > 5) return fail(QVMG_E_INVALID, "tile op width out of range");
-  if (s->prec == QVMG_FP64) return tile_launch<double>(s, args, smem);
-  return tile_launch<float>(s, args, smem);
+  if (s->prec == QVMG_FP64) {
+    if (args.R != 0) return fail(QVMG_E_INVALID, "register stages are FP32 only");
+    return tile_launch_r<double, 0>(s, args, smem);
+  }
+  if (args.R == 5) return tile_launch_r<float, 5>(s, args, smem);
+  if (args.R == 4) return tile_launch_r<float, 4>(s, args, smem);
+  if (args.R == 0) return tile_launch_r<float, 0>(s, args, smem);
+  return fail(QVMG_E_INVALID, "unsupported register-stage width");
 }
 
 }  // namespace qvmg

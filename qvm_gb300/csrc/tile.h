@@ -17,22 +17,37 @@ struct TileOpDev {
   int data;  // offset (complex elements) of the matrix / table in pass data
   int nmoved;
   int pos[10];  // dense/perm: tile-local bit positions; diag: global qubits (nat order)
+  int slot0, slot1;  // register-stage ops: register slots of pos[0], pos[1] (ascending)
   unsigned char src[32];
   unsigned char dst[32];
 };
-static_assert(sizeof(TileOpDev) == 120, "TileOpDev layout");
+static_assert(sizeof(TileOpDev) == 128, "TileOpDev layout");
+
+// One stage of a tile pass (80 bytes): a register run or one shared-memory op.
+struct TileStageDev {
+  int reg;    // 1: register run of ops [first, first+count)
+  int first;
+  int count;
+  int pad;
+  int slots[6];   // tile bits of register slots, ascending
+  int tpos[10];   // tile bits of thread-index bits, ascending
+};
+static_assert(sizeof(TileStageDev) == 80, "TileStageDev layout");
 
 struct TileArgs {
   int t, L, nE, nops;
   int E[kTileMaxE];  // global qubit of tile bit L+e, ascending
   int ndata;         // complex elements of op data
   int kmax;          // widest dense/permutation op of the pass (1..5)
+  int nstages;
+  int R;             // register bits of the register stages (0: none)
   unsigned long long ntiles;
-  const void *ops;   // TileOpDev[nops] in device memory
-  const void *data;  // complex op data in device memory (state precision)
+  const void *ops;     // TileOpDev[nops] in device memory
+  const void *data;    // complex op data in device memory (state precision)
+  const void *stages;  // TileStageDev[nstages] in device memory
 };
 
-size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops);
+size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages);
 int launch_tile(qvmg_state s, const TileArgs &args);
 
 }  // namespace qvmg

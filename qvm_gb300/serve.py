@@ -171,6 +171,14 @@ class Server:
                     self.reserved -= need
                 self.cv.notify_all()
 
+    def close_now(self):
+        """Cancel the queued requests, let running ones finish, free states."""
+        with self.cv:
+            while self.queue:
+                _, fut, _ = self.queue.popleft()
+                fut.cancel()
+        self.close()
+
     def close(self):
         with self.cv:
             self.stop = True

@@ -224,6 +224,10 @@ class Program:
             self.add_dense(m, qs)
         return self
 
+    def set_register_stages(self, enable: bool):
+        """Apply runs of 1-/2-qubit blocks in registers inside FP32 tiles."""
+        L.call("qvmg_program_set_option", self._h, 1, 1 if enable else 0)
+
     def num_ops(self) -> int:
         n = ctypes.c_int()
         L.call("qvmg_program_num_ops", self._h, ctypes.byref(n))

@@ -77,19 +77,22 @@ def _oracle_run(oracle, n, gs, init):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-@pytest.mark.parametrize("fw,tile", [(1, 0), (2, 0), (3, 6), (4, 9), (5, 10), (2, 7)])
+@pytest.mark.parametrize("fw,tile", [(1, 0), (2, 0), (3, 6), (4, 9), (5, 10), (2, 7), (2, 12),
+                                     (2, 13)])
 def test_fused_plan_equals_circuit(oracle, prec, fw, tile):
-    n = 11
+    n = 14
     for name, gs in [("su", circuits.random_su_circuit(n, depth=4, seed=fw * 7 + tile)),
                      ("layers", circuits.random_layers(n, layers=3, seed=5)),
                      ("qft", circuits.qft(n))]:
         init = circuits.random_state(n, seed=9)
         want = _oracle_run(oracle, n, gs, init)
         p = _program(gs)
-        st = p.plan(n, prec, fused=True, fusion_width=fw, tile_qubits=tile)
-        got = run_description(oracle, p.describe(), init.copy())
-        assert np.max(np.abs(got - want)) < 1e-12, (name, st)
-        assert st["source_ops"] == len(gs)
+        for reg in (False, True):
+            p.set_register_stages(reg)
+            st = p.plan(n, prec, fused=True, fusion_width=fw, tile_qubits=tile)
+            got = run_description(oracle, p.describe(), init.copy())
+            assert np.max(np.abs(got - want)) < 1e-12, (name, reg, st)
+            assert st["source_ops"] == len(gs)
 
 
 def test_plain_plan_equals_circuit(oracle):
@@ -103,6 +106,39 @@ def test_plain_plan_equals_circuit(oracle):
     assert np.max(np.abs(got - want)) < 1e-12
     # QFT: the CPHASE chain after each H is folded into phase passes
     assert st["diag_passes"] >= 1 and st["passes"] < len(gs)
+
+
+def test_register_stages_cover_their_ops():
+    """Every op of a register stage lies in the stage's slots, stages cover
+    the pass's ops in order, and the FP32 13-qubit tile uses 5 slots."""
+    n = 22
+    gs = circuits.random_su_circuit(n, depth=6, seed=4) + circuits.qft(n)
+    p = _program(gs)
+    p.plan(n, "fp32", fused=True, fusion_width=2, tile_qubits=13)
+    assert all(ps.get("R", 0) == 0 for ps in p.describe()["passes"])  # off by default
+    p.set_register_stages(True)
+    p.plan(n, "fp32", fused=True, fusion_width=2, tile_qubits=13)
+    d = p.describe()
+    nreg = 0
+    for ps in d["passes"]:
+        if ps["kind"] != "tile":
+            continue
+        assert ps["R"] == 5
+        nxt = 0
+        for st in ps["stages"]:
+            assert st["first"] == nxt
+            nxt += st["count"]
+            if st["reg"]:
+                nreg += 1
+                assert len(st["slots"]) == 5
+                for op in ps["ops"][st["first"]:st["first"] + st["count"]]:
+                    assert op["kind"] == "dense" and len(op["pos"]) <= 2
+                    assert set(op["pos"]) <= set(st["slots"])
+                    assert op["pos"] == sorted(op["pos"])
+        assert nxt == len(ps["ops"])
+    assert nreg > 0
+    p.plan(n, "fp64", fused=True, fusion_width=2, tile_qubits=12)
+    assert all(ps.get("R", 0) == 0 for ps in p.describe()["passes"])
 
 
 def test_fusion_reduces_passes():

@@ -128,9 +128,10 @@ def test_standard_gates(gpu, oracle, prec):
     s.free()
 
 
-def _run_program(gs, n, prec, fused, init=None, fw=2, tile=0):
+def _run_program(gs, n, prec, fused, init=None, fw=2, tile=0, reg=False):
     p = Program()
     p.add_gates(gs)
+    p.set_register_stages(reg)
     if fused:
         p.plan(n, prec, fused=True, fusion_width=fw, tile_qubits=tile)
     s = CudaPureState(n, prec)
@@ -184,6 +185,22 @@ def test_random_su_fused(gpu, oracle, prec, fw, tile):
     s = _run_program(gs, n, prec, True, fw=fw, tile=tile)
     got = s.state_elements()
     assert np.max(np.abs(got - want)) < tol(prec) * 2
+    s.free()
+
+
+@pytest.mark.parametrize("tile", [12, 13])
+def test_register_stages(gpu, oracle, tile):
+    """FP32 tiles with register stages (16 or 32 amplitudes per thread),
+    mixed with shared-memory ops (diagonal, permutation, 3-qubit blocks)."""
+    n = 18
+    rng = np.random.default_rng(tile)
+    gs = circuits.random_su_circuit(n, depth=5, seed=tile) + circuits.qft(n)
+    gs += [(gates.gate_matrix("CCNOT"), [int(x) for x in rng.choice(n, 3, replace=False)]),
+           (gates.haar_unitary(rng, 8), [int(x) for x in rng.choice(n, 3, replace=False)])]
+    gs += circuits.random_layers(n, layers=2, seed=tile)
+    want = _oracle(oracle, gs, n)
+    s = _run_program(gs, n, "fp32", True, fw=3, tile=tile, reg=True)
+    assert np.max(np.abs(s.state_elements() - want)) < 4e-6
     s.free()
 
 
