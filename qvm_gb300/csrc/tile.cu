@@ -49,6 +49,13 @@ __host__ __device__ __forceinline__ unsigned swz(unsigned j) {
   return j ^ ((((j >> 4) ^ (j >> 7) ^ (j >> 10)) & 7u) << 1);
 }
 
+// Tile index -> shared-memory index: swizzled only in kernels with register
+// stages (their gathers need it); the shared-memory ops alone do not.
+template <bool S>
+__device__ __forceinline__ unsigned sw(unsigned j) {
+  return S ? swz(j) : j;
+}
+
 __device__ __forceinline__ unsigned inject0u(unsigned x, int q) {
   unsigned lo = x & ((1u << q) - 1u);
   return ((x >> q) << (q + 1)) | lo;
@@ -56,7 +63,7 @@ __device__ __forceinline__ unsigned inject0u(unsigned x, int q) {
 
 // ---- shared-memory ops -----------------------------------------------------------
 
-template <typename T, int K>
+template <typename T, int K, bool S>
 __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const TileOpDev &op,
                                            const typename CT<T>::C *mat) {
   using C = typename CT<T>::C;
@@ -89,18 +96,18 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
     C v[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) v[c] = tile[swz(b | off[c])];
+    for (int c = 0; c < D; ++c) v[c] = tile[sw<S>(b | off[c])];
 #pragma unroll
     for (int r = 0; r < D; ++r) {
       C acc = CT<T>::make(0, 0);
 #pragma unroll
       for (int c = 0; c < D; ++c) cmac(acc, mat[r * D + c], v[c]);
-      tile[swz(b | off[r])] = acc;
+      tile[sw<S>(b | off[r])] = acc;
     }
   }
 }
 
-template <typename T, int K>
+template <typename T, int K, bool S>
 __device__ __forceinline__ void tile_perm(typename CT<T>::C *tile, int t, const TileOpDev &op) {
   using C = typename CT<T>::C;
   constexpr int D = 1 << K;
@@ -134,14 +141,14 @@ __device__ __forceinline__ void tile_perm(typename CT<T>::C *tile, int t, const 
     C v[D];
 #pragma unroll
     for (int j = 0; j < D; ++j)
-      if (j < nm) v[j] = tile[swz(b | off[op.src[j]])];
+      if (j < nm) v[j] = tile[sw<S>(b | off[op.src[j]])];
 #pragma unroll
     for (int j = 0; j < D; ++j)
-      if (j < nm) tile[swz(b | off[op.dst[j]])] = v[j];
+      if (j < nm) tile[sw<S>(b | off[op.dst[j]])] = v[j];
   }
 }
 
-template <typename T>
+template <typename T, bool S>
 __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
                                           const unsigned long long *rowoff, const TileOpDev &op,
                                           const typename CT<T>::C *table) {
@@ -155,7 +162,7 @@ __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
     for (int i = 0; i < k; ++i) idx |= (int)((g >> op.pos[i]) & 1ull) << i;
     C ph = table[idx];
     if (ph.x != (T)1 || ph.y != (T)0) {
-      const unsigned p = swz(j);
+      const unsigned p = sw<S>(j);
       tile[p] = cmul(tile[p], ph);
     }
   }
@@ -262,28 +269,28 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
   for (int r = 0; r < (1 << R); ++r) tile[lo[r & 3] ^ hi[r >> 2]] = v[r];
 }
 
-template <typename T, int KMAX>
+template <typename T, int KMAX, bool S>
 __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
                                         const unsigned long long *rowoff, const TileOpDev &op,
                                         const typename CT<T>::C *md) {
   if (op.kind == 0) {
     switch (op.k) {
-      case 1: tile_dense<T, 1>(tile, t, op, md); break;
-      case 2: tile_dense<T, 2>(tile, t, op, md); break;
-      case 3: if constexpr (KMAX >= 3) tile_dense<T, 3>(tile, t, op, md); break;
-      case 4: if constexpr (KMAX >= 4) tile_dense<T, 4>(tile, t, op, md); break;
-      case 5: if constexpr (KMAX >= 5) tile_dense<T, 5>(tile, t, op, md); break;
+      case 1: tile_dense<T, 1, S>(tile, t, op, md); break;
+      case 2: tile_dense<T, 2, S>(tile, t, op, md); break;
+      case 3: if constexpr (KMAX >= 3) tile_dense<T, 3, S>(tile, t, op, md); break;
+      case 4: if constexpr (KMAX >= 4) tile_dense<T, 4, S>(tile, t, op, md); break;
+      case 5: if constexpr (KMAX >= 5) tile_dense<T, 5, S>(tile, t, op, md); break;
     }
   } else if (op.kind == 2) {
     switch (op.k) {
-      case 1: tile_perm<T, 1>(tile, t, op); break;
-      case 2: tile_perm<T, 2>(tile, t, op); break;
-      case 3: if constexpr (KMAX >= 3) tile_perm<T, 3>(tile, t, op); break;
-      case 4: if constexpr (KMAX >= 4) tile_perm<T, 4>(tile, t, op); break;
-      case 5: if constexpr (KMAX >= 5) tile_perm<T, 5>(tile, t, op); break;
+      case 1: tile_perm<T, 1, S>(tile, t, op); break;
+      case 2: tile_perm<T, 2, S>(tile, t, op); break;
+      case 3: if constexpr (KMAX >= 3) tile_perm<T, 3, S>(tile, t, op); break;
+      case 4: if constexpr (KMAX >= 4) tile_perm<T, 4, S>(tile, t, op); break;
+      case 5: if constexpr (KMAX >= 5) tile_perm<T, 5, S>(tile, t, op); break;
     }
   } else {
-    tile_diag<T>(tile, t, L, rowoff, op, md);
+    tile_diag<T, S>(tile, t, L, rowoff, op, md);
   }
 }
 
@@ -336,7 +343,7 @@ __global__ void __launch_bounds__(kTileThreads, RB == 5 ? 2 : (KMAX <= 2 ? 3 : 1
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
       const C *src = a + rowoff[el >> L] + (el & rowmask);
-      cp_async16(tile + swz(el), src);
+      cp_async16(tile + sw<(RB > 0)>(el), src);
     }
     cp_async_wait_all();
     __syncthreads();
@@ -351,13 +358,13 @@ __global__ void __launch_bounds__(kTileThreads, RB == 5 ? 2 : (KMAX <= 2 ? 3 : 1
         }
       }
       const TileOpDev &op = ops[st.first];
-      smem_op<T, KMAX>(tile, t, L, rowoff, op, data + op.data);
+      smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data);
       __syncthreads();
     }
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
       int4 *dst = reinterpret_cast<int4 *>(a + rowoff[el >> L] + (el & rowmask));
-      __stcs(dst, *reinterpret_cast<const int4 *>(tile + swz(el)));
+      __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB > 0)>(el)));
     }
   }
 }

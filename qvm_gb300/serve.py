@@ -7,9 +7,12 @@ per request to release foreign memory.  Here requests are admitted onto the
 GPU by HBM bytes (16*2^n for FP64, 8*2^n for FP32, plus scratch) within a
 budget; every admitted request runs on its own state and CUDA stream, so the
 device overlaps the work of many requests; a request that arrives while
-others run is admitted as soon as a worker and enough memory are free
-(first fit from the queue, so a small request is not stuck behind a large
-one).  Freed states are kept in a pool keyed by (qubits, precision) and
+others run is admitted as soon as a worker and enough memory are free.
+Among the queued requests the cheapest one that fits goes first (estimated
+cost = gates x 2^n, FP64 weighted by its slower arithmetic, divided by an
+aging factor that grows with the wait), so small requests are not stuck
+behind a 30-qubit FP64 job and large ones still progress.  Freed states are
+kept in a pool keyed by (qubits, precision) and
 reused, evicted least-recently-used when admission needs their bytes.
 
 Each request's result depends only on its own program and draws: states are
@@ -88,8 +91,9 @@ class StatePool:
 
 
 class Server:
-    def __init__(self, hbm_budget: float = 180e9, workers: int = 16):
+    def __init__(self, hbm_budget: float = 180e9, workers: int = 16, aging_s: float = 2.0):
         self.budget = int(hbm_budget)
+        self.aging_s = float(aging_s)
         self.reserved = 0              # bytes of running requests + idle pooled states
         self.pool = StatePool()
         self.queue = collections.deque()
@@ -110,10 +114,25 @@ class Server:
             self.cv.notify()
         return fut
 
+    @staticmethod
+    def cost(req: Request) -> float:
+        """Estimated device work: gates x amplitudes, FP64 weighted by its
+        slower arithmetic on this part."""
+        return len(req.gates) * float(1 << req.n) * (8.0 if req.precision == "fp64" else 1.0)
+
+    def _order(self):
+        """Queue positions, cheapest first with aging: a request's cost is
+        divided by (1 + wait / aging_s), so large jobs are not starved."""
+        now = time.perf_counter()
+        score = [self.cost(r) / (1.0 + max(0.0, now - r.arrival) / self.aging_s)
+                 for r, _, _ in self.queue]
+        return sorted(range(len(self.queue)), key=score.__getitem__)
+
     def _admit(self):
-        """First queued request that fits (evicting idle pooled states if that
-        makes it fit).  Called with the lock held."""
-        for i, (req, fut, need) in enumerate(self.queue):
+        """The cheapest (aged) queued request that fits, evicting idle pooled
+        states if that makes it fit.  Called with the lock held."""
+        for i in self._order():
+            req, fut, need = self.queue[i]
             key_state = self.pool.take(req.n, req.precision)
             if key_state is not None:
                 del self.queue[i]

@@ -141,6 +141,25 @@ def test_register_stages_cover_their_ops():
     assert all(ps.get("R", 0) == 0 for ps in p.describe()["passes"])
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_tile_passes_fit_shared_memory(prec):
+    """Large QFTs fold many phase tables into a pass: every pass must still
+    fit the 227 KiB shared-memory limit of one CTA."""
+    csz = 16 if prec == "fp64" else 8
+    for n in (21, 25, 30):
+        p = _program(circuits.qft(n))
+        p.plan(n, prec, fused=True, fusion_width=2)
+        for ps in p.describe()["passes"]:
+            if ps["kind"] != "tile":
+                continue
+            t, L = ps["t"], ps["L"]
+            nd = sum(len(o["data"]) for o in ps["ops"] if o["kind"] != "perm")
+            rows = ((1 << (t - L)) + 1) & ~1
+            smem = (1 << t) * csz + rows * 8 + nd * csz + len(ps["ops"]) * 128 + \
+                len(ps["stages"]) * 80
+            assert smem <= 227 * 1024, (n, smem)
+
+
 def test_fusion_reduces_passes():
     n = 30
     gs = circuits.random_su_circuit(n, depth=20, seed=3)
