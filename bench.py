@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--shots", type=int, default=4096)
     ap.add_argument("--fw", type=int, default=0, help="fusion width (0: autotune)")
     ap.add_argument("--tile", type=int, default=0, help="tile qubits (0: autotune)")
-    ap.add_argument("--reg", type=int, default=-1, help="register stages 0/1 (-1: autotune)")
+    ap.add_argument("--engine", default="auto", choices=["auto", "fma", "reg"],
+                    help="tile engine: FP32 FMAs or register stages (auto: tune)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched QAOA run")
@@ -276,15 +277,15 @@ def main():
     s32 = CudaPureState(n, "fp32")
     stream = torch.cuda.ExternalStream(s32.stream())
     tuned = None
-    if args.fw == 0 or args.tile == 0 or args.reg < 0:
-        # untimed: pick fusion width, tile width and register stages for this
+    from qvm_gb300.autotune import DEFAULT_CANDIDATES, apply_engine, autotune
+    if args.fw == 0 or args.tile == 0 or args.engine == "auto":
+        # untimed: pick fusion width, tile width and tile engine for this
         # circuit on this GPU
-        from qvm_gb300.autotune import DEFAULT_CANDIDATES, autotune
-        cands = [(fw, t, r) for fw, t, r in DEFAULT_CANDIDATES["fp32"]
-                 if args.fw in (0, fw) and args.tile in (0, t) and args.reg in (-1, r)]
-        (args.fw, args.tile, args.reg), table = autotune(prog, s32, "fp32", cands)
-        tuned = {f"fw{fw}_t{t}_r{r}": round(ms, 2) for (fw, t, r), ms in sorted(table.items())}
-    prog.set_register_stages(bool(args.reg))
+        cands = [(fw, t, e) for fw, t, e in DEFAULT_CANDIDATES["fp32"]
+                 if args.fw in (0, fw) and args.tile in (0, t) and args.engine in ("auto", e)]
+        (args.fw, args.tile, args.engine), table = autotune(prog, s32, "fp32", cands)
+        tuned = {f"fw{fw}_t{t}_{e}": round(ms, 2) for (fw, t, e), ms in sorted(table.items())}
+    apply_engine(prog, args.engine)
     stats = prog.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
 
     def step():
@@ -331,7 +332,7 @@ def main():
         "workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth {args.depth}, {G} gates, "
                     f"fused FP32 (fusion width {args.fw})",
         "passes": stats["passes"], "fused_blocks": stats["fused_blocks"],
-        "fusion_width": args.fw, "tile_qubits": args.tile, "register_stages": args.reg,
+        "fusion_width": args.fw, "tile_qubits": args.tile, "tile_engine": args.engine,
         "autotune_ms": tuned,
         "state_bytes": state_bytes,
         "l2": "state (%.1f GiB) is larger than L2; no flush needed" % (state_bytes / 2 ** 30),
@@ -358,7 +359,7 @@ def main():
         t0 = time.perf_counter()
         p = Program()
         p.add_gates(gates)               # host gate matrices
-        p.set_register_stages(bool(args.reg))
+        apply_engine(p, args.engine)
         st = p.plan(n, "fp32", fused=True, fusion_width=args.fw, tile_qubits=args.tile)
         s32.set_to_zero_state()
         p.run(s32, fused=True)           # plan upload + passes

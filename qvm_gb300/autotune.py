@@ -1,10 +1,11 @@
-"""Autotuner for the fused path: fusion width, tile width and register stages.
+"""Autotuner for the fused path: fusion width, tile width and tile engine.
 
 For a program and a state size it plans and runs every candidate
-(fusion width, tile qubits, register stages on/off) once on the device,
-times the runs with the per-pass CUDA events of ``Program.run_profiled``,
-and keeps the fastest.  Results are cached in memory per
-(program id, qubits, precision).
+(fusion width, tile qubits, engine) once on the device, times the runs with
+the per-pass CUDA events of ``Program.run_profiled``, and keeps the fastest.
+Engines of an FP32 tile: "fma" (every block through shared memory on FP32
+FMAs) and "reg" (runs of 1-/2-qubit blocks on amplitudes held in registers).
+Results are cached in memory per (program id, qubits, precision).
 """
 from __future__ import annotations
 
@@ -12,28 +13,34 @@ import numpy as np
 
 from .state import CudaPureState, Program
 
+ENGINES = ("fma", "reg")
+
 DEFAULT_CANDIDATES = {
-    "fp32": [(fw, t, reg) for fw in (1, 2, 3) for t in (12, 13, 14) for reg in (0, 1)
-             if not (reg and t == 14)],
-    "fp64": [(fw, t, 0) for fw in (1, 2, 3) for t in (11, 12, 13)],
+    "fp32": [(fw, t, e) for fw in (1, 2) for t in (12, 13, 14) for e in ENGINES
+             if not (e == "reg" and t == 14)],
+    "fp64": [(fw, t, "fma") for fw in (1, 2, 3) for t in (11, 12, 13)],
 }
 
 _cache: dict = {}
 
 
+def apply_engine(prog: Program, engine: str):
+    prog.set_register_stages(engine == "reg")
+
+
 def autotune(prog: Program, state: CudaPureState, precision: str = "fp32", candidates=None,
              repeats: int = 1):
-    """Pick (fusion_width, tile_qubits, register_stages) for `prog` on
-    `state`; returns (best, table) with table[candidate] = device ms per run.
-    The state is overwritten (it is reset before every trial)."""
+    """Pick (fusion_width, tile_qubits, engine) for `prog` on `state`;
+    returns (best, table) with table[candidate] = device ms per run.  The
+    state is overwritten (it is reset before every trial)."""
     n = state.num_qubits()
     key = (id(prog), n, precision)
     if key in _cache:
         return _cache[key]
     table = {}
-    for fw, tile, reg in candidates or DEFAULT_CANDIDATES[precision]:
+    for fw, tile, engine in candidates or DEFAULT_CANDIDATES[precision]:
         try:
-            prog.set_register_stages(bool(reg))
+            apply_engine(prog, engine)
             prog.plan(n, precision, fused=True, fusion_width=fw, tile_qubits=tile)
         except Exception:
             continue
@@ -42,9 +49,9 @@ def autotune(prog: Program, state: CudaPureState, precision: str = "fp32", candi
             state.set_to_zero_state()
             ms, _ = prog.run_profiled(state, fused=True)
             best = min(best, float(ms.sum()))
-        table[(fw, tile, reg)] = best
+        table[(fw, tile, engine)] = best
     choice = min(table, key=table.get)
-    prog.set_register_stages(bool(choice[2]))
+    apply_engine(prog, choice[2])
     prog.plan(n, precision, fused=True, fusion_width=choice[0], tile_qubits=choice[1])
     _cache[key] = (choice, table)
     return choice, table

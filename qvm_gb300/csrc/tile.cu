@@ -89,6 +89,17 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
       if ((c >> j) & 1) o |= 1u << op.pos[j];
     off[c] = o;
   }
+  // Small matrices (FP32 1-/2-qubit, FP64 1-qubit) are held in registers
+  // across the group loop: 16 shared-memory loads per group saved for an
+  // FP32 2-qubit block.  Wider ones, and every matrix in the kernels with
+  // register stages (whose register budget those stages take), are read from
+  // shared memory with broadcast loads.
+  constexpr bool kHoist = !S && D * D * sizeof(C) <= 128;
+  C mreg[kHoist ? D * D : 1];
+  if constexpr (kHoist) {
+#pragma unroll
+    for (int i = 0; i < D * D; ++i) mreg[i] = mat[i];
+  }
   const unsigned ngroups = 1u << (t - K);
   for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
     unsigned b = g;
@@ -101,7 +112,10 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
     for (int r = 0; r < D; ++r) {
       C acc = CT<T>::make(0, 0);
 #pragma unroll
-      for (int c = 0; c < D; ++c) cmac(acc, mat[r * D + c], v[c]);
+      for (int c = 0; c < D; ++c) {
+        if constexpr (kHoist) cmac(acc, mreg[r * D + c], v[c]);
+        else cmac(acc, mat[r * D + c], v[c]);
+      }
       tile[sw<S>(b | off[r])] = acc;
     }
   }
