@@ -118,6 +118,21 @@ int qvmg_apply_permutation(qvmg_state s, int k, const int *qubits, const int64_t
  * sub-index j is multiplied by diag[j] (2^k complex128); k <= 10. */
 int qvmg_apply_diagonal(qvmg_state s, int k, const int *qubits, const double *diag);
 
+/* ---- noise on pure states -------------------------------------------------- */
+/* Reduced density matrix of k = 1 or 2 qubits: rho[r][c] (2^k x 2^k
+ * complex128, row-major) = sum of a_r conj(a_c) over the other qubits, with
+ * bit j of r <-> qubits[j].  Deterministic reduction order. */
+int qvmg_reduced_density_matrix(qvmg_state s, int k, const int *qubits, double *rho);
+/* %evolve-pure-state-stochastically (src/apply-gate.lisp:16-39): a Kraus map
+ * of `nops` operators (each 2^k x 2^k complex128, row-major, stored one
+ * after another) on k = 1 or 2 qubits.  Picks the first j whose running sum
+ * of p_i = ||K_i psi||^2 reaches `draw` (the last operator if rounding
+ * leaves the sum short), then replaces the state by K_j psi / sqrt(p_j).
+ * *chosen and *probability (may be NULL) receive j and p_j.  QVMG_E_RANGE if
+ * the selected p_j is zero. */
+int qvmg_apply_kraus(qvmg_state s, int k, const int *qubits, int nops, const double *ops,
+                     double draw, int *chosen, double *probability);
+
 /* ---- measurement (src/measurement.lisp) ----------------------------------- */
 /* wavefunction-excited-state-probability (src/wavefunction.lisp:62-70),
  * get-excited-state-probability (src/measurement.lisp:71-75); FP64 sum. */
@@ -166,6 +181,35 @@ int qvmg_sample_noalloc(const void *amps, int nqubits, int precision, const doub
                         uint64_t nshots, int rule, uint64_t *out, void *stream);
 /* |a_i|^2 for every amplitude (app/src/api/probabilities.lisp:13-19). */
 int qvmg_probabilities(qvmg_state s, double *out);
+/* Marginal distribution of k <= 20 distinct qubits: out[m] (2^k doubles) is
+ * the sum of |a_i|^2 over the i whose bit qubits[j] equals bit j of m.  One
+ * read of the state; the sums are deterministic (fixed reduction order). */
+int qvmg_marginal_probabilities(qvmg_state s, int k, const int *qubits, double *out);
+/* Repeated measurement of a resident state without collapsing it: the
+ * trials of multishot-measure (app/src/api/multishot-measure.lisp:12-35,
+ * 93-109), each of which reloads the prepared state and measures
+ * qubits[0..k-1] in order with measure (src/measurement.lisp:87-105;
+ * convention QVMG_MEASURE_INTERPRETED: a draw is taken only when p1 != 0,
+ * bit = draw <= p1) or the compiled measurement
+ * (src/compile-gate.lisp:221-254; QVMG_MEASURE_COMPILED: a draw every time,
+ * bit = 0 iff draw < p0).  A qubit of -1 is an unused slot (bit 0, no draw);
+ * a repeated qubit reads its earlier outcome.  At most 20 distinct qubits
+ * (measuring every qubit is the measure-all path: qvmg_sample with
+ * QVMG_SAMPLE_BISECT).  Draws are consumed in trial order, then list order;
+ * bits[t*k + e] receives trial t, entry e; *draws_used the number consumed
+ * (QVMG_E_RANGE when `ndraws` runs out).  The state is not modified. */
+int qvmg_measure_sequence(qvmg_state s, int k, const int *qubits, int convention, int ntrials,
+                          const double *draws, uint64_t ndraws, uint8_t *bits,
+                          uint64_t *draws_used);
+/* Wire bytes of the wavefunction endpoint (app/src/handle-request.lisp:
+ * 132-152, write-complex-double-float-as-binary in app/src/utilities.lisp:
+ * 62-77): per amplitude, the real then the imaginary part as IEEE doubles in
+ * big-endian byte order; `out` holds 16 * 2^n octets. */
+int qvmg_wavefunction_octets(qvmg_state s, uint8_t *out);
+/* Wire bytes of the probabilities endpoint (app/src/handle-request.lisp:
+ * 154-175, write-double-float-as-binary in app/src/utilities.lisp:79-87):
+ * |a_i|^2 as big-endian IEEE doubles; `out` holds 8 * 2^n octets. */
+int qvmg_probabilities_octets(qvmg_state s, uint8_t *out);
 /* norm / normalize-wavefunction (src/wavefunction.lisp:332-364). */
 int qvmg_norm(qvmg_state s, double *norm);
 int qvmg_normalize(qvmg_state s);

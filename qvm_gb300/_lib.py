@@ -54,6 +54,12 @@ SIGNATURES = {
     "qvmg_sample": (_i, [_vp, _dp, _u64, _i, _u64p]),
     "qvmg_sample_noalloc": (_i, [_vp, _i, _i, _vp, _u64, _i, _vp, _vp]),
     "qvmg_probabilities": (_i, [_vp, _dp]),
+    "qvmg_marginal_probabilities": (_i, [_vp, _i, _ip, _dp]),
+    "qvmg_reduced_density_matrix": (_i, [_vp, _i, _ip, _dp]),
+    "qvmg_apply_kraus": (_i, [_vp, _i, _ip, _i, _dp, ctypes.c_double, _ip, _dp]),
+    "qvmg_measure_sequence": (_i, [_vp, _i, _ip, _i, _i, _dp, _u64, _vp, _u64p]),
+    "qvmg_wavefunction_octets": (_i, [_vp, _vp]),
+    "qvmg_probabilities_octets": (_i, [_vp, _vp]),
     "qvmg_norm": (_i, [_vp, _dp]),
     "qvmg_normalize": (_i, [_vp]),
     "qvmg_inner": (_i, [_vp, _vp, _dp, _dp]),

@@ -122,6 +122,24 @@ class CudaPureState:
         d = _cplx(diag)
         L.call("qvmg_apply_diagonal", self.handle, len(qubits), _qubit_array(qubits), _dptr(d))
 
+    # -- noise ---------------------------------------------------------------------
+    def reduced_density_matrix(self, qubits) -> np.ndarray:
+        """rho of 1 or 2 qubits (nat order: bit j of an index <-> qubits[j])."""
+        d = 1 << len(qubits)
+        out = np.empty((d, d), dtype=np.complex128)
+        L.call("qvmg_reduced_density_matrix", self.handle, len(qubits), _qubit_array(qubits),
+               _dptr(out))
+        return out
+
+    def apply_kraus(self, kraus_ops, qubits, draw: float):
+        """Stochastic Kraus map on 1 or 2 qubits; returns (chosen index, p_j)."""
+        ops = np.ascontiguousarray(np.stack([_cplx(k) for k in kraus_ops]))
+        chosen = ctypes.c_int(-1)
+        prob = ctypes.c_double(0.0)
+        L.call("qvmg_apply_kraus", self.handle, len(qubits), _qubit_array(qubits), len(ops),
+               _dptr(ops), float(draw), ctypes.byref(chosen), ctypes.byref(prob))
+        return chosen.value, prob.value
+
     # -- measurement -------------------------------------------------------------
     def excited_probability(self, q: int) -> float:
         p = ctypes.c_double()
@@ -164,6 +182,38 @@ class CudaPureState:
         out = np.empty(1 << self._n, dtype=np.float64)
         L.call("qvmg_probabilities", self.handle, _dptr(out))
         return out
+
+    def marginal_probabilities(self, qubits) -> np.ndarray:
+        """out[m] = P(bit qubits[j] = bit j of m for every j); <= 20 qubits."""
+        out = np.empty(1 << len(qubits), dtype=np.float64)
+        L.call("qvmg_marginal_probabilities", self.handle, len(qubits), _qubit_array(qubits),
+               _dptr(out))
+        return out
+
+    def measure_sequence(self, qubits, draws, ntrials: int, compiled: bool = False):
+        """Measure ``qubits`` in order (-1 = unused slot) on ``ntrials``
+        reloads of this state; returns (bits[ntrials, len(qubits)], draws
+        consumed).  The state is not modified."""
+        d = np.ascontiguousarray(draws, dtype=np.float64)
+        bits = np.zeros((int(ntrials), len(qubits)), dtype=np.uint8)
+        used = ctypes.c_uint64(0)
+        conv = L.MEASURE_COMPILED if compiled else L.MEASURE_INTERPRETED
+        L.call("qvmg_measure_sequence", self.handle, len(qubits), _qubit_array(qubits), conv,
+               int(ntrials), _dptr(d), len(d), bits.ctypes.data_as(ctypes.c_void_p),
+               ctypes.byref(used))
+        return bits, int(used.value)
+
+    def wavefunction_octets(self) -> bytes:
+        """The amplitudes as big-endian complex doubles (16 octets each)."""
+        out = np.empty(16 << self._n, dtype=np.uint8)
+        L.call("qvmg_wavefunction_octets", self.handle, out.ctypes.data_as(ctypes.c_void_p))
+        return out.tobytes()
+
+    def probabilities_octets(self) -> bytes:
+        """|a_i|^2 as big-endian doubles (8 octets each)."""
+        out = np.empty(8 << self._n, dtype=np.uint8)
+        L.call("qvmg_probabilities_octets", self.handle, out.ctypes.data_as(ctypes.c_void_p))
+        return out.tobytes()
 
     def norm(self) -> float:
         n = ctypes.c_double()
