@@ -132,6 +132,14 @@ int qvmg_reduced_density_matrix(qvmg_state s, int k, const int *qubits, double *
  * the selected p_j is zero. */
 int qvmg_apply_kraus(qvmg_state s, int k, const int *qubits, int nops, const double *ops,
                      double draw, int *chosen, double *probability);
+/* A density matrix of n qubits held as the 2n-qubit vector vec(rho), row
+ * major (density-matrix-state, src/state-representation.lisp:173-266):
+ * gates, Kraus maps (as the superoperator sum_j K_j (x) conj(K_j)),
+ * measurement collapse and dephasing are ordinary 2n-qubit ops on it.  This
+ * reads its diagonal: out[i] = Re rho[i][i] (2^n doubles), the outcome
+ * distribution of density-matrix-state-measurement-probabilities
+ * (src/state-representation.lisp:268-290). */
+int qvmg_density_diagonal(qvmg_state s, double *out);
 
 /* ---- measurement (src/measurement.lisp) ----------------------------------- */
 /* wavefunction-excited-state-probability (src/wavefunction.lisp:62-70),

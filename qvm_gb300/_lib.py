@@ -56,6 +56,7 @@ SIGNATURES = {
     "qvmg_probabilities": (_i, [_vp, _dp]),
     "qvmg_marginal_probabilities": (_i, [_vp, _i, _ip, _dp]),
     "qvmg_reduced_density_matrix": (_i, [_vp, _i, _ip, _dp]),
+    "qvmg_density_diagonal": (_i, [_vp, _dp]),
     "qvmg_apply_kraus": (_i, [_vp, _i, _ip, _i, _dp, ctypes.c_double, _ip, _dp]),
     "qvmg_measure_sequence": (_i, [_vp, _i, _ip, _i, _i, _dp, _u64, _vp, _u64p]),
     "qvmg_wavefunction_octets": (_i, [_vp, _vp]),

@@ -1,4 +1,4 @@
-// noise.cu -- stochastic Kraus maps on a pure state.
+// noise.cu -- stochastic Kraus maps on a pure state; density-matrix diagonals.
 //
 // The reference's noisy QVM applies a noisy gate, given as a Kraus map
 // {K_j}, to a pure state by inverse transform sampling
@@ -159,6 +159,18 @@ static double kraus_probability(const double *K, const std::vector<double> &rho,
   return total;
 }
 
+// ---- density matrices stored as 2n-qubit vectors ------------------------------------
+//
+// vec(rho) is row-major (src/state-representation.lisp:173-188,235-266):
+// entry (i, j) of the 2^n x 2^n matrix is amplitude i * 2^n + j, so the
+// diagonal is the stride-(2^n + 1) slice.
+template <typename C>
+__global__ void k_density_diagonal(const C *__restrict__ a, uint64_t dim, double *__restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = (double)a[i * (dim + 1)].x;
+}
+
 }  // namespace qvmg
 
 using namespace qvmg;
@@ -173,6 +185,26 @@ int qvmg_reduced_density_matrix(qvmg_state s, int k, const int *qubits, double *
   std::vector<double> r;
   if ((rc = reduced_density_matrix(s, k, qubits, r))) return rc;
   std::copy(r.begin(), r.end(), rho);
+  return QVMG_OK;
+}
+
+int qvmg_density_diagonal(qvmg_state s, double *out) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if (!out) return fail(QVMG_E_INVALID, "null output");
+  if (s->nq % 2) return fail(QVMG_E_INVALID, "a density matrix needs an even qubit count");
+  const uint64_t dim = 1ull << (s->nq / 2);
+  if ((rc = ensure_staging(s, dim * sizeof(double)))) return rc;
+  if (s->prec == QVMG_FP64)
+    k_density_diagonal<double2><<<grid_for(dim, 256), 256, 0, s->stream>>>(
+        (const double2 *)s->amps, dim, (double *)s->staging);
+  else
+    k_density_diagonal<float2><<<grid_for(dim, 256), 256, 0, s->stream>>>(
+        (const float2 *)s->amps, dim, (double *)s->staging);
+  QVMG_CHECK_LAUNCH("k_density_diagonal");
+  QVMG_CUDA(cudaMemcpyAsync(out, s->staging, dim * sizeof(double), cudaMemcpyDeviceToHost,
+                            s->stream));
+  QVMG_CUDA(cudaStreamSynchronize(s->stream));
   return QVMG_OK;
 }
 

@@ -131,6 +131,12 @@ class CudaPureState:
                _dptr(out))
         return out
 
+    def density_diagonal(self) -> np.ndarray:
+        """Re rho[i][i] of a density matrix held as vec(rho) (2n qubits)."""
+        out = np.empty(1 << (self._n // 2), dtype=np.float64)
+        L.call("qvmg_density_diagonal", self.handle, _dptr(out))
+        return out
+
     def apply_kraus(self, kraus_ops, qubits, draw: float):
         """Stochastic Kraus map on 1 or 2 qubits; returns (chosen index, p_j)."""
         ops = np.ascontiguousarray(np.stack([_cplx(k) for k in kraus_ops]))
