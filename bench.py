@@ -46,8 +46,9 @@ def parse():
     ap.add_argument("--shots", type=int, default=4096)
     ap.add_argument("--fw", type=int, default=0, help="fusion width (0: autotune)")
     ap.add_argument("--tile", type=int, default=0, help="tile qubits (0: autotune)")
-    ap.add_argument("--engine", default="auto", choices=["auto", "fma", "reg"],
-                    help="tile engine: FP32 FMAs or register stages (auto: tune)")
+    ap.add_argument("--engine", default="auto", choices=["auto", "fma", "reg", "tc"],
+                    help="tile engine: FP32 FMAs, register stages or tcgen05 tensor cores "
+                         "(auto: tune)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched QAOA run")
@@ -78,6 +79,18 @@ def max_over_ranks(value: float) -> float:
 def whole_job_rate(units_per_rank_step: int, steps: int, world: int, max_ms: float) -> float:
     """Units all ranks processed divided by the slowest rank's time."""
     return world * units_per_rank_step * steps / (max_ms / 1e3)
+
+
+# DRAM bytes (read + write) of one fused FP32 tile launch at 26 qubits, from
+# the ncu captures summarised under profiles/ (k_tile_fp32_random26_fw2_t13,
+# k_tile_tc_fp32_random26_fw4_t13).  Traffic per launch grows with the
+# amplitudes processed, so a launch at n qubits moves 2^(n-26) times as much.
+TILE_TRAFFIC_26Q = {"fma": 536.917504e6 + 475.407360e6, "tc": 536.962816e6 + 478.344448e6}
+
+
+def traffic_per_launch(n, engine):
+    b = TILE_TRAFFIC_26Q.get(engine)
+    return None if b is None else b * 2.0 ** (n - 26)
 
 
 def peaks():
@@ -347,7 +360,10 @@ def main():
                               "peak": peak, "unit": "GB/s", "frac": ach / peak,
                               "peak_source": peak_kind,
                               "algorithmic_bytes_per_launch": 2 * state_bytes,
-                              "avg_launch_ms": avg, "traffic": None}
+                              "avg_launch_ms": avg,
+                              "traffic": traffic_per_launch(n, args.engine),
+                              "traffic_source": "ncu dram__bytes_read+write of one 26-qubit "
+                                                "launch of the same engine, scaled by 2^(n-26)"}
     result["gpu_launches"] = launches
     result["clocks"] = clk
 

@@ -250,6 +250,11 @@ int qvmg_program_plan(qvmg_program p, int nqubits, int precision, int mode,
  * blocks to amplitudes held in registers inside a tile (FP32, 12/13-qubit
  * tiles), 0 = every block through shared memory (default). */
 #define QVMG_OPT_REGISTER_STAGES 1
+/* QVMG_OPT_TENSOR_CORES: 1 = in FP32 tiles, merge each pass's dense blocks
+ * into blocks of up to 4 qubits and run the 3- and 4-qubit ones on the
+ * tensor cores (tcgen05 TF32 MMAs, operands split into hi + lo TF32 parts,
+ * three products accumulated in FP32), 0 = CUDA-core FMAs (default). */
+#define QVMG_OPT_TENSOR_CORES 2
 int qvmg_program_set_option(qvmg_program p, int option, int value);
 /* Plan statistics: stats[0]=source ops, [1]=passes, [2]=tile passes,
  * [3]=fused blocks, [4]=diagonal passes, [5]=permutation passes,

@@ -4,7 +4,8 @@ For a program and a state size it plans and runs every candidate
 (fusion width, tile qubits, engine) once on the device, times the runs with
 the per-pass CUDA events of ``Program.run_profiled``, and keeps the fastest.
 Engines of an FP32 tile: "fma" (every block through shared memory on FP32
-FMAs) and "reg" (runs of 1-/2-qubit blocks on amplitudes held in registers).
+FMAs), "reg" (runs of 1-/2-qubit blocks on amplitudes held in registers) and
+"tc" (blocks merged to 3-4 qubits and run as tcgen05 TF32 MMAs).
 Results are cached in memory per (program id, qubits, precision).
 """
 from __future__ import annotations
@@ -13,11 +14,11 @@ import numpy as np
 
 from .state import CudaPureState, Program
 
-ENGINES = ("fma", "reg")
+ENGINES = ("fma", "reg", "tc")
 
 DEFAULT_CANDIDATES = {
-    "fp32": [(fw, t, e) for fw in (1, 2) for t in (12, 13, 14) for e in ENGINES
-             if not (e == "reg" and t == 14)],
+    "fp32": [(fw, t, e) for fw in (1, 2) for t in (12, 13, 14) for e in ("fma", "reg")
+             if not (e == "reg" and t == 14)] + [(4, 12, "tc"), (4, 13, "tc"), (2, 13, "tc")],
     "fp64": [(fw, t, "fma") for fw in (1, 2, 3) for t in (11, 12, 13)],
 }
 
@@ -26,6 +27,7 @@ _cache: dict = {}
 
 def apply_engine(prog: Program, engine: str):
     prog.set_register_stages(engine == "reg")
+    prog.set_tensor_cores(engine == "tc")
 
 
 def autotune(prog: Program, state: CudaPureState, precision: str = "fp32", candidates=None,

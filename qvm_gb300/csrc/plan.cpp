@@ -24,6 +24,7 @@
 #include "plan.h"
 
 #include <algorithm>
+#include <cstring>
 #include <set>
 #include <stdexcept>
 
@@ -299,7 +300,8 @@ size_t tile_pass_smem_bytes(const Pass &p, int prec) {
   size_t csz = prec == QVMG_FP64 ? 16 : 8;
   size_t rows = (((size_t)1 << (p.t - p.L)) + 1) & ~(size_t)1;
   size_t b = ((size_t)1 << p.t) * csz + rows * 8;
-  for (auto &o : p.tops) b += o.data.size() * csz + kTileOpDescBytes;
+  // (+ csz: a tensor-core operand starts on a 16-byte boundary)
+  for (auto &o : p.tops) b += o.data.size() * csz + kTileOpDescBytes + (o.kind == OP_TC ? csz : 0);
   b += p.stages.size() * kTileStageDescBytes;
   return (b + 15) & ~(size_t)15;
 }
@@ -404,7 +406,9 @@ static void plan_fused(const std::vector<Op> &ops, int nq, int prec, int fw, int
         p.tops.push_back(std::move(top));
       }
       flush();
-      build_stages(p, prec, plan.reg_stages);
+      const bool tc = plan.tensor_cores && prec == QVMG_FP32;
+      if (tc) merge_tile_ops(p, kTcMaxQubits, true);
+      build_stages(p, prec, plan.reg_stages && !tc);
       return p;
     };
     Pass p = build_pass(in_pass);
@@ -416,6 +420,104 @@ static void plan_fused(const std::vector<Op> &ops, int nq, int prec, int fw, int
     }
     plan.passes.push_back(std::move(p));
     plan.n_tile++;
+  }
+}
+
+// ---- tensor-core ops ---------------------------------------------------------------
+
+// TF32 rounding of an FP32 value: round to nearest, ties away from zero (the
+// device's cvt.rna.tf32.f32), kept as an FP32 value with 13 zero low bits.
+static float tf32_rna(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
+std::vector<float> tc_operand(const std::vector<cd> &m, int k) {
+  const int D = 1 << k, N = 2 * D, K = 2 * D;
+  std::vector<float> out((size_t)2 * N * K, 0.f);
+  for (int n = 0; n < N; ++n)
+    for (int kk = 0; kk < K; ++kk) {
+      const int r = n >> 1, c = kk >> 1;
+      const cd z = m[(size_t)r * D + c];
+      double x;
+      if ((n & 1) == 0) x = (kk & 1) == 0 ? z.real() : -z.imag();
+      else x = (kk & 1) == 0 ? z.imag() : z.real();
+      const float hi = tf32_rna((float)x);
+      const float lo = tf32_rna((float)(x - (double)hi));
+      const size_t idx = (size_t)((n >> 3) * (K >> 2) + (kk >> 2)) * 32 + (n & 7) * 4 + (kk & 3);
+      out[idx] = hi;
+      out[(size_t)N * K + idx] = lo;
+    }
+  return out;
+}
+
+// Global qubits an op of a tile pass touches.
+static std::vector<int> op_globals(const Pass &p, const TileOpHost &o) {
+  if (o.kind == OP_DIAG) return o.pos;
+  std::vector<int> g;
+  for (int b : o.pos) g.push_back(b < p.L ? b : p.E[b - p.L]);
+  return g;
+}
+
+void merge_tile_ops(Pass &p, int maxk, bool tensor_cores) {
+  std::vector<TileOpHost> out;
+  for (TileOpHost &op : p.tops) {
+    if (op.kind != OP_DENSE || (int)op.pos.size() > maxk) {
+      out.push_back(std::move(op));
+      continue;
+    }
+    const std::vector<int> g = op_globals(p, op);
+    int target = -1;
+    for (int i = (int)out.size() - 1; i >= 0; --i) {
+      const TileOpHost &z = out[i];
+      const std::vector<int> gz = op_globals(p, z);
+      bool overlap = false;
+      for (int q : g)
+        if (std::find(gz.begin(), gz.end(), q) != gz.end()) overlap = true;
+      if (z.kind == OP_DENSE) {
+        std::set<int> u(z.pos.begin(), z.pos.end());
+        u.insert(op.pos.begin(), op.pos.end());
+        if ((int)u.size() <= maxk) {
+          target = i;
+          break;
+        }
+      }
+      if (overlap) break;  // op cannot move before z
+    }
+    if (target < 0) {
+      out.push_back(std::move(op));
+      continue;
+    }
+    // z' = op . z over the union of their tile bits (op runs after z, and
+    // commutes with every op between them)
+    TileOpHost &z = out[target];
+    std::vector<int> bq = z.pos;
+    for (int b : op.pos)
+      if (std::find(bq.begin(), bq.end(), b) == bq.end()) bq.push_back(b);
+    Op oz, oo;
+    oz.kind = oo.kind = OP_DENSE;
+    oz.q = z.pos;
+    oz.m = z.data;
+    oo.q = op.pos;
+    oo.m = op.data;
+    const int db = 1 << (int)bq.size();
+    z.data = matmul(embed(oo, bq), embed(oz, bq), db);
+    z.pos = bq;
+  }
+  p.tops.swap(out);
+  if (!tensor_cores) return;
+  for (TileOpHost &op : p.tops) {
+    const int k = (int)op.pos.size();
+    if (op.kind != OP_DENSE || k < kTcMinQubits || k > kTcMaxQubits) continue;
+    if ((1 << (p.t - k)) < kTcRows) continue;  // fewer than 128 groups
+    const std::vector<float> f = tc_operand(op.data, k);
+    op.kind = OP_TC;
+    op.data.resize(f.size() / 2);
+    for (size_t i = 0; i < op.data.size(); ++i) op.data[i] = cd(f[2 * i], f[2 * i + 1]);
   }
 }
 
@@ -493,9 +595,10 @@ void build_stages(Pass &p, int prec, bool reg_stages) {
 }
 
 void make_plan(const std::vector<Op> &ops, int nq, int prec, int mode, int fw, int tile,
-               Plan &plan, bool reg_stages) {
+               Plan &plan, bool reg_stages, bool tensor_cores) {
   plan = Plan();
   plan.reg_stages = reg_stages;
+  plan.tensor_cores = tensor_cores;
   plan.nq = nq;
   plan.prec = prec;
   plan.mode = mode;

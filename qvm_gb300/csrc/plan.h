@@ -9,7 +9,13 @@ namespace qvmg {
 
 using cd = std::complex<double>;
 
-enum OpKind { OP_DENSE = 0, OP_DIAG = 1, OP_PERM = 2 };
+enum OpKind { OP_DENSE = 0, OP_DIAG = 1, OP_PERM = 2, OP_TC = 3 };
+
+// Tensor-core tile ops: dense blocks of kTcMinQubits..kTcMaxQubits tile
+// bits run as tcgen05 TF32 MMAs over chunks of 128 groups.
+constexpr int kTcMinQubits = 3;
+constexpr int kTcMaxQubits = 4;
+constexpr int kTcRows = 128;
 
 // One gate application (or fused block).  Qubits are in nat-tuple order:
 // q[j] is bit j of the matrix index.
@@ -24,9 +30,10 @@ struct Op {
 // Tile-local op: the unit of work inside a shared-memory tile pass.
 struct TileOpHost {
   int kind;
-  std::vector<int> pos;      // dense/perm: tile-local bit positions (nat order)
+  std::vector<int> pos;      // dense/perm/tc: tile-local bit positions (nat order)
                              // diag: global qubits (nat order)
-  std::vector<cd> data;      // dense matrix, or diag table
+  std::vector<cd> data;      // dense matrix, or diag table; tc: the split real
+                             // form (tc_operand), two floats per element
   std::vector<int64_t> perm; // perm moves
 };
 
@@ -56,11 +63,12 @@ struct Pass {
   std::vector<TileStage> stages;
 };
 
-// Device descriptor sizes of tile ops and stages (tile.h), and the shared
-// memory one tile pass may use (227 KiB per CTA on sm_103a).
+// Device descriptor sizes of tile ops and stages (tile.h), and the dynamic
+// shared memory one tile pass may use (227 KiB per CTA on sm_103a, less 64
+// bytes for the kernel's static shared variables).
 constexpr size_t kTileOpDescBytes = 128;
 constexpr size_t kTileStageDescBytes = 80;
-constexpr size_t kTileSmemBudget = 227 * 1024;
+constexpr size_t kTileSmemBudget = 227 * 1024 - 64;
 size_t tile_pass_smem_bytes(const Pass &p, int prec);
 
 // Register bits per thread for a tile of t qubits run by 256 threads:
@@ -74,15 +82,27 @@ void build_stages(Pass &p, int prec, bool reg_stages);
 struct Plan {
   int nq = -1, prec = -1, mode = -1, fw = -1, tile = -1;
   bool reg_stages = false;
+  bool tensor_cores = false;
   std::vector<Pass> passes;
   int64_t n_src = 0, n_blocks = 0, n_tile = 0, n_diag = 0, n_perm = 0, n_dense = 0;
 };
+
+// Tensor-core operand of a dense k-qubit block (k = 3, 4): the real form
+// Bt[n][kk] (n = 2r + re/im of output r, kk = 2c + re/im of input c), split
+// into TF32 hi and lo parts (round to nearest, ties away), each laid out
+// K-major in 8x4 core matrices: element (n, kk) at float
+// ((n/8)*(2D/4) + kk/4)*32 + (n%8)*4 + kk%4; hi block, then lo block.
+std::vector<float> tc_operand(const std::vector<cd> &m, int k);
+// Merge a tile pass's dense ops into blocks of at most `maxk` tile bits
+// (moving an op past ops on disjoint qubits), then turn the blocks that fit
+// the tensor-core path into OP_TC ops.
+void merge_tile_ops(Pass &p, int maxk, bool tensor_cores);
 
 // Gate fusion: merge consecutive gates into blocks of at most `fw` qubits.
 std::vector<Op> fuse_ops(const std::vector<Op> &ops, int fw);
 // Build a plan for a state of nq qubits.
 void make_plan(const std::vector<Op> &ops, int nq, int prec, int mode, int fw, int tile,
-               Plan &plan, bool reg_stages = false);
+               Plan &plan, bool reg_stages = false, bool tensor_cores = false);
 // Default tile width (qubits held per tile) for a precision.
 int default_tile_qubits(int prec);
 int tile_low_bits(int prec);

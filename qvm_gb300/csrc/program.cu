@@ -8,6 +8,8 @@
 // runs the fused + tiled plan.
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -26,6 +28,7 @@ namespace qvmg {
 static_assert(sizeof(TileOpDev) == kTileOpDescBytes, "planner op descriptor size");
 static_assert(sizeof(TileStageDev) == kTileStageDescBytes, "planner stage descriptor size");
 static_assert(kTileMaxSmem == (int)kTileSmemBudget, "planner shared-memory budget");
+static_assert(kTileTcRows == kTcRows, "tensor-core chunk rows");
 
 // Device image of one plan for one precision.
 struct DevicePlan {
@@ -35,6 +38,7 @@ struct DevicePlan {
   std::vector<TileArgs> tile_args;      // per pass (TILE passes)
   std::vector<std::vector<int>> dks;    // per pass (DIAG passes): table widths
   std::vector<std::vector<int>> dqs;    // per pass (DIAG passes): flat qubits
+  bool has_tc = false;                  // some tile pass runs tensor-core ops
   ~DevicePlan() {
     if (buf) cudaFree(buf);
   }
@@ -45,12 +49,14 @@ struct DevicePlan {
 struct qvmg_program_s {
   std::vector<qvmg::Op> ops;
   std::mutex mu;
-  // key: (nq, prec, mode, fw, tile, register stages)
-  std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<qvmg::DevicePlan>> plans;
+  // key: (nq, prec, mode, fw, tile, register stages, tensor cores)
+  std::map<std::tuple<int, int, int, int, int, int, int>, std::unique_ptr<qvmg::DevicePlan>>
+      plans;
   qvmg::Plan last_plan;  // most recent host-only plan (for statistics)
   int default_fw = 2;
   int default_tile = 0;
   int reg_stages = 0;
+  int tensor_cores = 0;
 };
 
 namespace qvmg {
@@ -72,7 +78,8 @@ static void align16(std::vector<unsigned char> &bytes) {
 
 static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw, int tile,
                              DevicePlan &dp, cudaStream_t stream) {
-  make_plan(p->ops, nq, prec, mode, fw, tile, dp.plan, p->reg_stages != 0);
+  make_plan(p->ops, nq, prec, mode, fw, tile, dp.plan, p->reg_stages != 0,
+            p->tensor_cores != 0);
   std::vector<unsigned char> bytes;
   const size_t csz = prec == QVMG_FP64 ? 16 : 8;
   dp.pass_off.assign(dp.plan.passes.size(), 0);
@@ -111,8 +118,16 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
         d.kind = th.kind;
         d.k = (int)th.pos.size();
         for (int j = 0; j < d.k; ++j) d.pos[j] = th.pos[j];
+        if (th.kind == OP_TC && (ndata & 1)) {  // 16-byte aligned operand
+          data.push_back(cd(0, 0));
+          ++ndata;
+        }
         d.data = ndata;
-        if (th.kind != OP_DIAG) ta.kmax = std::max(ta.kmax, d.k);
+        if (th.kind == OP_TC) {
+          ta.tc = 1;
+          dp.has_tc = true;
+        }
+        else if (th.kind != OP_DIAG) ta.kmax = std::max(ta.kmax, d.k);
         if (th.kind == OP_PERM) {
           int nm = 0;
           for (size_t j = 0; j < th.perm.size(); ++j)
@@ -221,9 +236,26 @@ static int run_device_plan(qvmg_state s, DevicePlan &dp, cudaEvent_t *events = n
         rc = launch_diag_dev(s, (int)dp.dks[i].size(), dp.dks[i].data(), dp.dqs[i].data(),
                              (const unsigned char *)dp.buf + dp.pass_off[i]);
         break;
-      case Pass::TILE:
-        rc = launch_tile(s, dp.tile_args[i]);
+      case Pass::TILE: {
+        TileArgs ta = dp.tile_args[i];
+        ta.status = reinterpret_cast<int *>(reinterpret_cast<char *>(s->dres) +
+                                            offsetof(MeasResult, status));
+        rc = launch_tile(s, ta);
         break;
+      }
+    }
+  }
+  if (dp.has_tc && rc == QVMG_OK) {
+    // a tensor-core pass whose bounded MMA wait gave up has set the status word
+    int *dstatus = reinterpret_cast<int *>(reinterpret_cast<char *>(s->dres) +
+                                           offsetof(MeasResult, status));
+    QVMG_CUDA(cudaMemcpyAsync(&s->hres->status, dstatus, sizeof(int), cudaMemcpyDeviceToHost,
+                              s->stream));
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->hres->status != 0) {
+      s->hres->status = 0;
+      QVMG_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), s->stream));
+      return fail(QVMG_E_TIMEOUT, "a tensor-core tile pass timed out waiting for its MMAs");
     }
   }
   if (events && rc == QVMG_OK)
@@ -323,7 +355,10 @@ static std::string describe_plan(const Plan &pl) {
         const TileOpHost &th = ps.tops[o];
         if (o) s += ",";
         s += std::string("{\"kind\":\"") +
-             (th.kind == OP_DENSE ? "dense" : th.kind == OP_DIAG ? "diag" : "perm") +
+             (th.kind == OP_DENSE  ? "dense"
+              : th.kind == OP_DIAG ? "diag"
+              : th.kind == OP_TC   ? "tc"
+                                   : "perm") +
              "\",\"pos\":";
         ints(th.pos);
         if (th.kind == OP_PERM) {
@@ -442,7 +477,7 @@ int qvmg_program_plan(qvmg_program p, int nqubits, int precision, int mode, int 
   if (program_max_qubit(p) > nqubits)
     return fail(QVMG_E_INVALID, "program uses a qubit beyond the state's qubit count");
   make_plan(p->ops, nqubits, precision, mode, fusion_width, tile_qubits, p->last_plan,
-            p->reg_stages != 0);
+            p->reg_stages != 0, p->tensor_cores != 0);
   p->default_fw = fusion_width;
   p->default_tile = tile_qubits;
   if (npasses) *npasses = (int)p->last_plan.passes.size();
@@ -452,6 +487,11 @@ int qvmg_program_plan(qvmg_program p, int nqubits, int precision, int mode, int 
 int qvmg_program_set_option(qvmg_program p, int option, int value) {
   if (!p) return fail(QVMG_E_INVALID, "null program");
   std::lock_guard<std::mutex> g(p->mu);
+  if (option == QVMG_OPT_TENSOR_CORES) {
+    if (value != 0 && value != 1) return fail(QVMG_E_INVALID, "tensor-core option is 0 or 1");
+    p->tensor_cores = value;
+    return QVMG_OK;
+  }
   if (option == QVMG_OPT_REGISTER_STAGES) {
     if (value != 0 && value != 1) return fail(QVMG_E_INVALID, "register stages option is 0 or 1");
     p->reg_stages = value;
@@ -501,7 +541,7 @@ static int device_plan_for(qvmg_state s, qvmg_program p, int mode, DevicePlan **
     return fail(QVMG_E_INVALID, "program uses a qubit beyond the state's qubit count");
   int fw = mode == QVMG_RUN_FUSED ? p->default_fw : 1;
   int tile = mode == QVMG_RUN_FUSED ? p->default_tile : 0;
-  auto key = std::make_tuple(s->nq, s->prec, mode, fw, tile, p->reg_stages);
+  auto key = std::make_tuple(s->nq, s->prec, mode, fw, tile, p->reg_stages, p->tensor_cores);
   auto it = p->plans.find(key);
   if (it == p->plans.end()) {
     auto dp = std::make_unique<DevicePlan>();

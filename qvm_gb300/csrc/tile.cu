@@ -283,6 +283,225 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
   for (int r = 0; r < (1 << R); ++r) tile[lo[r & 3] ^ hi[r >> 2]] = v[r];
 }
 
+// ---- tensor-core ops (FP32, tcgen05) ---------------------------------------------------
+//
+// A dense block on k = 3 or 4 tile bits is a real GEMM per chunk of 128
+// groups: D[g][n] = sum_kk A[g][kk] Bt[n][kk], with A[g] the group's 2^k
+// amplitudes as (re, im) pairs and Bt the block's real form (n = 2r + re/im
+// of output r).  Operands are split into TF32 hi + lo parts and
+// D = Ahi*Bhi + (Ahi*Blo + Alo*Bhi) is accumulated in FP32 in tensor memory,
+// the large product and the two small ones in separate columns that are
+// added on read-out.  A is written to tensor memory by the threads
+// (row g = TMEM lane g, one thread per row and half-row: warps w and w+4
+// share the lanes of sub-partition w%4 and take the two halves of the
+// group), Bt comes from the pass data in shared memory (split on the host,
+// K-major 8x4 core matrices).  A ninth warp issues the MMAs and commits
+// them to an mbarrier that the eight data warps wait on with a bounded loop.
+//
+// Chunks are software-pipelined over two TMEM buffer sets (each: D | A hi |
+// A lo) and two barriers: while the MMAs of chunk c are issued and run, the
+// data warps read out and scatter chunk c-1 and gather chunk c+1.
+constexpr int kTcCols = 256;           // TMEM columns per CTA: 2 buffers x 128
+constexpr int kTcBufCols = 128;
+constexpr int kTcWaitLimit = 1 << 22;  // polls of an MMA barrier before giving up
+
+struct TcCtx {
+  uint32_t tmem;      // TMEM address of lane 0, column 0 of this CTA's allocation
+  uint32_t mbar[2];   // shared addresses of the two MMA-completion barriers
+  uint32_t phase[2];  // parity of the phase each barrier's next wait is for
+  int ok;             // 0 once a wait gave up
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// Shared-memory matrix descriptor: K-major, no swizzle; the next 4-element
+// core matrix along K is 128 bytes on, the next 8 rows `sbo` bytes on.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+      "r"(a), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+template <int NR>
+__device__ __forceinline__ void tmem_st(uint32_t taddr, const uint32_t (&r)[NR]);
+template <>
+__device__ __forceinline__ void tmem_st<8>(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"r"(
+                   taddr),
+               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+               "r"(r[7]));
+}
+template <>
+__device__ __forceinline__ void tmem_st<16>(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15]));
+}
+
+template <int NR>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[NR]);
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+template <>
+__device__ __forceinline__ void tmem_ld<16>(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+// Bounded wait for the barrier phase of parity `phase`; 1 when it completed.
+__device__ __forceinline__ uint32_t tc_wait(uint32_t mbar, uint32_t phase) {
+  uint32_t done = 0;
+  for (int it = 0; it < kTcWaitLimit && !done; ++it)
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+  return done;
+}
+
+template <int K>
+__device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op, const float *bmat,
+                                        TcCtx &ctx, volatile int *abort_flag) {
+  constexpr int D = 1 << K, NC = 2 * D, H = D / 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool issuer = warp == kTileThreads / 32;  // the extra warp issues the MMAs
+  const int sub = warp & 3, half = (warp >> 2) & 1;
+  int sp[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) sp[i] = op.pos[i];
+#pragma unroll
+  for (int i = 1; i < K; ++i)
+#pragma unroll
+    for (int j = i; j > 0; --j)
+      if (sp[j - 1] > sp[j]) {
+        const int x = sp[j];
+        sp[j] = sp[j - 1];
+        sp[j - 1] = x;
+      }
+  unsigned off[H];  // this thread's half of the group: amplitudes half*H .. half*H + H-1
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const int c = half * H + i;
+    unsigned o = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if ((c >> j) & 1) o |= 1u << op.pos[j];
+    off[i] = o;
+  }
+  // Per buffer: columns [0, NC) = Ahi*Bhi, [NC, 2NC) = Ahi*Blo + Alo*Bhi,
+  // then A hi and A lo.  The operand's hi and lo blocks are consecutive
+  // 8-row groups, i.e. one K-major matrix [Bhi | Blo] of 2*NC rows, so
+  // Ahi*[Bhi | Blo] is a single MMA of N = 2*NC.
+  const uint32_t idesc_w = (1u << 4) | (2u << 7) | (2u << 10) |
+                           ((uint32_t)((2 * NC) >> 3) << 17) |
+                           ((uint32_t)(kTileTcRows >> 4) << 24);
+  const uint32_t idesc_n = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NC >> 3) << 17) |
+                           ((uint32_t)(kTileTcRows >> 4) << 24);
+  const uint32_t col_ahi = 2 * NC, col_alo = 3 * NC;
+  const uint32_t lanes = (uint32_t)(sub * 32) << 16;
+  const uint32_t bhi = smem_u32(bmat);
+  const uint32_t sbo = (NC / 4) * 128;
+  const unsigned nchunks = (1u << (t - K)) / kTileTcRows;
+  auto group_base = [&](unsigned ch) {
+    unsigned b = ch * kTileTcRows + sub * 32 + lane;
+#pragma unroll
+    for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
+    return b;
+  };
+  for (unsigned ch = 0; ch <= nchunks; ++ch) {
+    const uint32_t buf = ctx.tmem + (ch & 1u) * kTcBufCols;
+    if (!issuer && ch < nchunks) {
+      // gather + split chunk ch into this buffer's A columns (its previous
+      // MMAs, chunk ch-2, completed and were read out last iteration)
+      const unsigned b = group_base(ch);
+      uint32_t hi[D], lo[D];
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const float2 v = tile[b | off[i]];
+        hi[2 * i] = tf32_rna(v.x);
+        lo[2 * i] = tf32_rna(v.x - __uint_as_float(hi[2 * i]));
+        hi[2 * i + 1] = tf32_rna(v.y);
+        lo[2 * i + 1] = tf32_rna(v.y - __uint_as_float(hi[2 * i + 1]));
+      }
+      tmem_st<D>(buf + lanes + col_ahi + half * D, hi);
+      tmem_st<D>(buf + lanes + col_alo + half * D, lo);
+      asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (*abort_flag) {  // uniform: read after the barrier
+      ctx.ok = 0;
+      return;
+    }
+    if (issuer) {
+      if (ch < nchunks && lane == 0) {
+#pragma unroll
+        for (int s = 0; s < NC / 8; ++s) {
+          tc_mma(buf, buf + col_ahi + 8 * s, tc_desc(bhi + s * 256, sbo), idesc_w, s > 0);
+          tc_mma(buf + NC, buf + col_alo + 8 * s, tc_desc(bhi + s * 256, sbo), idesc_n, 1);
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                ctx.mbar[ch & 1u])
+            : "memory");
+      }
+    } else if (ch >= 1) {
+      // read out and scatter chunk ch-1 while chunk ch's MMAs are issued
+      const unsigned pb = (ch - 1) & 1u;
+      if (!tc_wait(ctx.mbar[pb], ctx.phase[pb])) {
+        *abort_flag = 1;  // seen by every thread after the next barrier
+        continue;
+      }
+      ctx.phase[pb] ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t pbuf = ctx.tmem + pb * kTcBufCols + lanes;
+      uint32_t r0[D], r1[D];
+      tmem_ld<D>(pbuf + half * D, r0);
+      tmem_ld<D>(pbuf + NC + half * D, r1);
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      const unsigned b = group_base(ch - 1);
+#pragma unroll
+      for (int i = 0; i < H; ++i)
+        tile[b | off[i]] =
+            make_float2(__uint_as_float(r0[2 * i]) + __uint_as_float(r1[2 * i]),
+                        __uint_as_float(r0[2 * i + 1]) + __uint_as_float(r1[2 * i + 1]));
+    }
+  }
+  __syncthreads();  // a wait that gave up on the last chunk is seen here
+  if (*abort_flag) ctx.ok = 0;
+}
+
 template <typename T, int KMAX, bool S>
 __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
                                         const unsigned long long *rowoff, const TileOpDev &op,
@@ -311,11 +530,36 @@ __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
 // KMAX: widest op of the pass; RB: register bits of the register stages
 // (0: every stage runs in shared memory).  Narrow instantiations keep the
 // register arrays of wide cases out of the kernel.
+// Threads of a tile CTA: 256, plus the MMA-issuing warp in tensor-core kernels.
+template <int RB>
+constexpr int tile_threads() {
+  return RB < 0 ? kTileThreads + 32 : kTileThreads;
+}
+
 template <typename T, int KMAX, int RB>
-__global__ void __launch_bounds__(kTileThreads, RB == 5 ? 2 : (KMAX <= 2 ? 3 : 1))
+__global__ void __launch_bounds__(tile_threads<RB>(), (RB == 5 || RB < 0) ? 2 : (KMAX <= 2 ? 3 : 1))
     k_tile(typename CT<T>::C *__restrict__ a, const __grid_constant__ TileArgs p) {
   using C = typename CT<T>::C;
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long tc_mbar[2];
+  __shared__ uint32_t tc_tmem_slot;
+  __shared__ int tc_abort;
+  TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1};
+  if constexpr (RB < 0) {
+    if ((threadIdx.x >> 5) == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                       smem_u32(&tc_tmem_slot)),
+                   "n"(kTcCols)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+      tc_abort = 0;
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[0])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[1])) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+  }
   const int t = p.t, L = p.L;
   C *tile = reinterpret_cast<C *>(smem);
   unsigned long long *rowoff = reinterpret_cast<unsigned long long *>(tile + (1u << t));
@@ -335,6 +579,16 @@ __global__ void __launch_bounds__(kTileThreads, RB == 5 ? 2 : (KMAX <= 2 ? 3 : 1
     int *st = reinterpret_cast<int *>(stages);
     const int swords = p.nstages * (int)(sizeof(TileStageDev) / 4);
     for (int i = threadIdx.x; i < swords; i += blockDim.x) st[i] = gt[i];
+  }
+  if constexpr (RB < 0) {
+    // the tensor core reads the operands in the pass data through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    ctx.tmem = tc_tmem_slot;
+    ctx.mbar[0] = smem_u32(&tc_mbar[0]);
+    ctx.mbar[1] = smem_u32(&tc_mbar[1]);
   }
   constexpr int per16 = 16 / sizeof(C);  // amplitudes per 16-byte chunk
   const unsigned nchunks = (1u << t) / per16;
@@ -372,14 +626,41 @@ __global__ void __launch_bounds__(kTileThreads, RB == 5 ? 2 : (KMAX <= 2 ? 3 : 1
         }
       }
       const TileOpDev &op = ops[st.first];
+      if constexpr (RB < 0) {
+        if (op.kind == 3) {
+          const float *bm = reinterpret_cast<const float *>(data + op.data);
+          if (op.k == 3) tile_tc<3>(reinterpret_cast<float2 *>(tile), t, op, bm, ctx, &tc_abort);
+          else tile_tc<4>(reinterpret_cast<float2 *>(tile), t, op, bm, ctx, &tc_abort);
+          if (!ctx.ok) break;
+          __syncthreads();
+          continue;
+        }
+      }
       smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data);
       __syncthreads();
+    }
+    if constexpr (RB < 0) {
+      if (!ctx.ok) break;  // uniform: set after a block-wide vote
     }
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
       int4 *dst = reinterpret_cast<int4 *>(a + rowoff[el >> L] + (el & rowmask));
       __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB > 0)>(el)));
     }
+  }
+  if constexpr (RB < 0) {
+    if (!ctx.ok) {
+      if (threadIdx.x == 0) atomicExch(p.status, 1);
+      // let MMAs still in flight finish (bounded) before their TMEM is freed
+      (void)tc_wait(ctx.mbar[0], ctx.phase[0]);
+      (void)tc_wait(ctx.mbar[1], ctx.phase[1]);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(ctx.tmem),
+                   "n"(kTcCols)
+                   : "memory");
   }
 }
 
@@ -397,16 +678,40 @@ static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
   if (!attr) {
     QVMG_CUDA(cudaFuncSetAttribute(k_tile<T, KMAX, RB>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, kTileMaxSmem));
+    // the whole unified L1/shared array as shared memory: the occupancy
+    // query (and the launch) then fit as many tiles per SM as the bytes allow
+    QVMG_CUDA(cudaFuncSetAttribute(k_tile<T, KMAX, RB>,
+                                   cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared));
     attr = true;
   }
   // Persistent grid: as many CTAs as fit on every SM at once (registers and
   // shared memory), each looping over tiles.
   int per_sm = 0;
   QVMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<T, KMAX, RB>,
-                                                          kTileThreads, smem));
+                                                          tile_threads<RB>(), smem));
   if (per_sm < 1) return fail(QVMG_E_UNSUPPORTED, "tile pass does not fit on an SM");
+  if (RB < 0) {
+    // The occupancy query answers 1 for kernels that allocate tensor memory;
+    // count what bounds co-resident CTAs ourselves: shared memory (with the
+    // 1 KiB the runtime reserves per CTA), registers, and the 512 TMEM
+    // columns of an SM.  (The persistent loop is correct for any grid.)
+    static int smem_sm = 0, regs = 0, stat = 0;
+    if (!smem_sm) {
+      int dev = 0;
+      QVMG_CUDA(cudaGetDevice(&dev));
+      QVMG_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+      cudaFuncAttributes fa;
+      QVMG_CUDA(cudaFuncGetAttributes(&fa, k_tile<T, KMAX, RB>));
+      regs = fa.numRegs;
+      stat = (int)fa.sharedSizeBytes;
+    }
+    const int by_smem = smem_sm / (int)(smem + (size_t)stat + 1024);
+    const int by_regs = 65536 / (((regs * 32 + 255) / 256) * 256 * (tile_threads<RB>() / 32));
+    per_sm = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTcCols));
+  }
   uint64_t grid = std::min<uint64_t>(args.ntiles, (uint64_t)sm_count() * per_sm);
-  k_tile<T, KMAX, RB><<<(unsigned)grid, kTileThreads, smem, s->stream>>>(
+  k_tile<T, KMAX, RB><<<(unsigned)grid, tile_threads<RB>(), smem, s->stream>>>(
       (typename CT<T>::C *)s->amps, args);
   QVMG_CHECK_LAUNCH("k_tile");
   return QVMG_OK;
@@ -426,6 +731,11 @@ int launch_tile(qvmg_state s, const TileArgs &args) {
   if (s->prec == QVMG_FP64) {
     if (args.R != 0) return fail(QVMG_E_INVALID, "register stages are FP32 only");
     return tile_launch_r<double, 0>(s, args, smem);
+  }
+  if (args.tc) {
+    if (args.R != 0) return fail(QVMG_E_INVALID, "tensor-core passes have no register stages");
+    if (!args.status) return fail(QVMG_E_INVALID, "tensor-core pass without a status word");
+    return tile_launch_r<float, -1>(s, args, smem);
   }
   if (args.R == 5) return tile_launch_r<float, 5>(s, args, smem);
   if (args.R == 4) return tile_launch_r<float, 4>(s, args, smem);

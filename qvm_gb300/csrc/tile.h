@@ -7,12 +7,15 @@
 namespace qvmg {
 
 constexpr int kTileThreads = 256;
-constexpr int kTileMaxSmem = 227 * 1024;
+// Dynamic shared memory of a tile pass: the 227 KiB a CTA may hold, less
+// 64 bytes for the kernel's static shared variables (MMA barrier, TMEM slot).
+constexpr int kTileMaxSmem = 227 * 1024 - 64;
 constexpr int kTileMaxE = 24;
+constexpr int kTileTcRows = 128;  // groups per tensor-core chunk (MMA M)
 
 // One op of a tile pass (128 bytes, copied into shared memory as words).
 struct TileOpDev {
-  int kind;  // 0 dense, 1 diagonal table, 2 permutation
+  int kind;  // 0 dense, 1 diagonal table, 2 permutation, 3 tensor-core dense
   int k;     // qubits
   int data;  // offset (complex elements) of the matrix / table in pass data
   int nmoved;
@@ -41,7 +44,10 @@ struct TileArgs {
   int kmax;          // widest dense/permutation op of the pass (1..5)
   int nstages;
   int R;             // register bits of the register stages (0: none)
+  int tc;            // 1: the pass has tensor-core ops (kind 3)
+  int pad;
   unsigned long long ntiles;
+  int *status;       // device status word: set on a bounded wait that gave up
   const void *ops;     // TileOpDev[nops] in device memory
   const void *data;    // complex op data in device memory (state precision)
   const void *stages;  // TileStageDev[nstages] in device memory

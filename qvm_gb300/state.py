@@ -284,6 +284,11 @@ class Program:
         """Apply runs of 1-/2-qubit blocks in registers inside FP32 tiles."""
         L.call("qvmg_program_set_option", self._h, 1, 1 if enable else 0)
 
+    def set_tensor_cores(self, enable: bool):
+        """Merge the dense blocks of FP32 tiles into blocks of up to 4 qubits
+        and run the 3- and 4-qubit ones on the tensor cores."""
+        L.call("qvmg_program_set_option", self._h, 2, 1 if enable else 0)
+
     def num_ops(self) -> int:
         n = ctypes.c_int()
         L.call("qvmg_program_num_ops", self._h, ctypes.byref(n))

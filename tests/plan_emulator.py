@@ -19,6 +19,22 @@ def _apply_table(wf, qubits, table):
     wf *= table[sub]
 
 
+def tc_matrix(pairs, k):
+    """The complex block of a tensor-core tile op from its operand: the TF32
+    hi + lo parts of the real form Bt (n = 2r + re/im of output r,
+    kk = 2c + re/im of input c), K-major 8x4 core matrices."""
+    f = np.array(pairs, dtype=np.float64).reshape(-1)
+    d = 1 << k
+    nk = 2 * d
+    n = np.arange(nk)[:, None]
+    kk = np.arange(nk)[None, :]
+    idx = ((n >> 3) * (nk >> 2) + (kk >> 2)) * 32 + (n & 7) * 4 + (kk & 3)
+    bt = f[idx] + f[nk * nk + idx]
+    re, im = bt[0::2, 0::2], bt[1::2, 0::2]
+    assert np.array_equal(bt[1::2, 1::2], re) and np.array_equal(bt[0::2, 1::2], -im)
+    return re + 1j * im
+
+
 def run_description(oracle, desc, wf):
     for p in desc["passes"]:
         kind = p["kind"]
@@ -38,6 +54,9 @@ def run_description(oracle, desc, wf):
                     _apply_table(wf, op["pos"], _cplx(op["data"]))
                 elif op["kind"] == "perm":
                     oracle.apply_permutation(wf, op["perm"], [glob(x) for x in op["pos"]])
+                elif op["kind"] == "tc":
+                    m = tc_matrix(op["data"], len(op["pos"]))
+                    oracle.apply_matrix_operator(wf, m, [glob(x) for x in op["pos"]])
                 else:
                     k = len(op["pos"])
                     m = _cplx(op["data"]).reshape(1 << k, 1 << k)

@@ -95,6 +95,35 @@ def test_fused_plan_equals_circuit(oracle, prec, fw, tile):
             assert st["source_ops"] == len(gs)
 
 
+@pytest.mark.parametrize("fw,tile", [(2, 0), (4, 0), (2, 11), (4, 12), (1, 13)])
+def test_tensor_core_plan_equals_circuit(oracle, fw, tile):
+    """FP32 tensor-core planning: the pass-local merge into blocks of <= 4
+    tile bits and the split TF32 operand, executed on the oracle, equal the
+    unfused circuit to the hi + lo precision (~2^-22 relative per block)."""
+    n = 16
+    for name, gs in [("su", circuits.random_su_circuit(n, depth=5, seed=fw + tile)),
+                     ("layers", circuits.random_layers(n, layers=3, seed=6)),
+                     ("qft", circuits.qft(n))]:
+        init = circuits.random_state(n, seed=3)
+        want = _oracle_run(oracle, n, gs, init)
+        p = _program(gs)
+        p.set_tensor_cores(True)
+        st = p.plan(n, "fp32", fused=True, fusion_width=fw, tile_qubits=tile)
+        d = p.describe()
+        tcs = [op for ps in d["passes"] if ps["kind"] == "tile" for op in ps["ops"]
+               if op["kind"] == "tc"]
+        if name != "qft":
+            assert tcs, name  # the random circuits produce 3-/4-qubit blocks
+        for op in tcs:
+            assert 3 <= len(op["pos"]) <= 4
+        got = run_description(oracle, d, init.copy())
+        assert np.max(np.abs(got - want)) < 2e-6, (name, st)
+        # FP64 plans never use the tensor cores
+        p.plan(n, "fp64", fused=True, fusion_width=fw, tile_qubits=tile)
+        assert not any(op["kind"] == "tc" for ps in p.describe()["passes"]
+                       if ps["kind"] == "tile" for op in ps["ops"])
+
+
 def test_plain_plan_equals_circuit(oracle):
     n = 9
     gs = circuits.qft(n) + circuits.random_layers(n, layers=2, seed=2)

@@ -128,10 +128,11 @@ def test_standard_gates(gpu, oracle, prec):
     s.free()
 
 
-def _run_program(gs, n, prec, fused, init=None, fw=2, tile=0, reg=False):
+def _run_program(gs, n, prec, fused, init=None, fw=2, tile=0, reg=False, tc=False):
     p = Program()
     p.add_gates(gs)
     p.set_register_stages(reg)
+    p.set_tensor_cores(tc)
     if fused:
         p.plan(n, prec, fused=True, fusion_width=fw, tile_qubits=tile)
     s = CudaPureState(n, prec)
@@ -202,6 +203,39 @@ def test_register_stages(gpu, oracle, tile):
     s = _run_program(gs, n, "fp32", True, fw=3, tile=tile, reg=True)
     assert np.max(np.abs(s.state_elements() - want)) < 4e-6
     s.free()
+
+
+@pytest.mark.parametrize("fw,tile", [(2, 13), (4, 13), (4, 12), (3, 11)])
+def test_tensor_core_tiles(gpu, oracle, fw, tile):
+    """FP32 tiles whose merged 3-/4-qubit blocks run as tcgen05 TF32 MMAs
+    (hi/lo split operands), mixed with 2-qubit FMA blocks, permutations and
+    diagonal tables.  The MMA accumulator rounds toward zero, which shrinks
+    the norm by ~1e-7 per block; the comparison is per amplitude (4e-6) and
+    as a normalised overlap (1 - 1e-6)."""
+    n = 18
+    rng = np.random.default_rng(tile + fw)
+    gs = circuits.random_su_circuit(n, depth=5, seed=tile) + circuits.qft(n)
+    gs += [(gates.gate_matrix("CCNOT"), [int(x) for x in rng.choice(n, 3, replace=False)]),
+           (gates.haar_unitary(rng, 8), [int(x) for x in rng.choice(n, 3, replace=False)])]
+    gs += circuits.random_layers(n, layers=2, seed=tile)
+    want = _oracle(oracle, gs, n)
+    s = _run_program(gs, n, "fp32", True, fw=fw, tile=tile, tc=True)
+    got = s.state_elements()
+    assert np.max(np.abs(got - want)) < 4e-6
+    assert abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real >= 1 - 1e-6
+    s.free()
+
+
+def test_tensor_core_fidelity_26q(gpu):
+    """Fused FP32 with the tensor-core engine vs plain FP64 at 26 qubits."""
+    n = 26
+    gs = circuits.random_su_circuit(n, depth=20, seed=3)
+    s64 = _run_program(gs, n, "fp64", False)
+    s32 = _run_program(gs, n, "fp32", True, fw=4, tile=13, tc=True)
+    f, err = s64.fidelity(s32)
+    assert f >= 1 - 1e-6 and err < 1e-5
+    s64.free()
+    s32.free()
 
 
 def test_small_states_all_paths(gpu, oracle):
