@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched QAOA run")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
+    ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit FP64 QFT")
+    ap.add_argument("--no-layers", action="store_true",
+                    help="skip the 20-qubit layer circuit with 1000 shots")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -201,6 +204,84 @@ def run_qaoa_batch(seed: int = 4, runs: int = 3):
            "h2d_bytes": int(draws.nbytes), "d2h_bytes": int(shots.nbytes + ex.nbytes)}
     b.free()
     return out
+
+
+def run_qft_fp64(n: int = 28, seed: int = 2, runs: int = 3):
+    """28-qubit QFT in complex FP64, plain kernels (one pass per H and SWAP,
+    one phase-table pass per CPHASE chain) on a random normalised state of
+    complex N(0,1) amplitudes.  Reports gates/s and HBM GB/s per pass kind,
+    from CUDA events around every pass.  Algorithmic bytes per pass: dense
+    and phase passes read and write every amplitude (2 * 16 * 2^n); a SWAP
+    moves half of them (2 * 16 * 2^(n-1))."""
+    from qvm_gb300 import CudaPureState, Program, circuits
+    gates = circuits.qft(n)
+    rng = np.random.default_rng(seed)
+    wf = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    wf /= np.linalg.norm(wf)
+    s = CudaPureState(n, "fp64")
+    s.set_state_elements(wf)
+    del wf
+    prog = Program()
+    prog.add_gates(gates)
+    st = prog.plan(n, "fp64", fused=False)
+    prog.run(s, fused=False)  # untimed: uploads the plan
+    s.sync()
+    amp = 16 * (1 << n)
+    bytes_of = {0: 2 * amp, 1: 2 * amp, 2: amp}   # dense, diagonal table, permutation
+    names = {0: "dense", 1: "phase", 2: "swap"}
+    best = None
+    for _ in range(runs):
+        ms, kinds = prog.run_profiled(s, fused=False)
+        if best is None or ms.sum() < best[0].sum():
+            best = (ms, kinds)
+    ms, kinds = best
+    peak, _ = peaks()
+    per = {}
+    for k in (0, 1, 2):
+        sel = kinds == k
+        if sel.any():
+            t = float(ms[sel].sum())
+            gbs = bytes_of[k] * int(sel.sum()) / (t / 1e3) / 1e9
+            per[names[k]] = {"passes": int(sel.sum()), "ms": t, "GB_per_s": gbs,
+                             "frac_of_measured_peak": gbs / peak}
+    total = float(ms.sum())
+    moved = sum(bytes_of[int(k)] for k in kinds)
+    s.free()
+    prog.free()
+    return {"workload": f"QFT, {n} qubits, complex FP64, plain kernels, random normalised state",
+            "gates": len(gates), "passes": st["passes"], "ms": total,
+            "gates_per_s": len(gates) / (total / 1e3),
+            "hbm_GB_per_s": moved / (total / 1e3) / 1e9,
+            "frac_of_measured_peak": moved / (total / 1e3) / 1e9 / peak, "per_pass_kind": per}
+
+
+def run_layers_shots(n: int = 20, layers: int = 10, shots: int = 1000, seed: int = 1, runs: int = 5):
+    """The plain small case: 20-qubit FP64 state, H on all qubits, 10 layers of
+    RX/RZ on every qubit and CNOTs on alternating pairs, then measure-all for
+    1000 shots (bisection rule on the reloaded state).  Timed end to end per
+    run from |0...0> to the downloaded shots."""
+    from qvm_gb300 import CudaPureState, Program, circuits
+    gates = circuits.random_layers(n, layers=layers, seed=seed)
+    s = CudaPureState(n, "fp64")
+    prog = Program()
+    prog.add_gates(gates)
+    draws = np.random.default_rng(seed).random(shots)
+    times = []
+    for i in range(runs + 1):
+        t0 = time.perf_counter()
+        s.set_to_zero_state()
+        prog.run(s, fused=False)
+        out = s.sample(draws, rule="bisect")
+        t1 = time.perf_counter()
+        if i:
+            times.append(t1 - t0)
+    dt = float(np.median(times))
+    s.free()
+    prog.free()
+    return {"workload": f"{n}-qubit RX/RZ/CNOT layers ({len(gates)} gates), FP64 plain kernels, "
+                        f"{shots} measure-all shots", "ms": 1e3 * dt,
+            "gates_per_s": len(gates) / dt, "shots_per_s": shots / dt,
+            "first_shots": [int(x) for x in out[:4]]}
 
 
 def run_serving(arrive_s: float = 1.5, drain_s: float = 60.0, seed: int = 5):
@@ -416,6 +497,10 @@ def main():
                               "shots": int(args.shots),
                               "identical_shots": int((sh64 == sh32).sum())}
         s64.free()
+    if not args.no_qft and rank == 0:
+        result["qft28_fp64"] = run_qft_fp64()
+    if not args.no_layers and rank == 0:
+        result["layers20_shots"] = run_layers_shots()
     if not args.no_batch and rank == 0:
         result["batch_qaoa"] = run_qaoa_batch()
     if not args.no_serve and rank == 0:

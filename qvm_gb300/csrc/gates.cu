@@ -10,10 +10,11 @@
 //    parameter bank (uniform across the warp), scatter back.  128-bit loads
 //    (one double2 / float2 per amplitude), grid-stride over groups.
 //  - k_perm<K>: only the amplitudes a permutation moves are read/written.
-//  - k_diag_tables: a run of diagonal gates is folded on the host into at
-//    most kMaxTables phase tables over <= 10 qubits each; each amplitude's
-//    phase is the product of its table entries; amplitudes whose phase is
-//    exactly 1 are neither read nor written.
+//  - k_diag_tables_f32 / _f64: a run of diagonal gates is folded on the host
+//    into at most kMaxTables phase tables over <= 10 qubits each (ascending
+//    qubits; a contiguous range is indexed by one shift and mask); each
+//    amplitude's phase is the product of its table entries other than 1;
+//    amplitudes whose entries are all 1 are neither read nor written.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -101,29 +102,132 @@ struct DiagArgs {
   int k[kMaxTables];
   int qubits[kMaxTables][kMaxTableBits];
   int start[kMaxTables];  // entry offset of each table
+  // Ascending qubits that form at most two contiguous runs, lo1 .. lo1+n1-1
+  // then lo2 .. lo2+k-n1-1 (lo1 = -1: any other set, gathered bit by bit).
+  // A CPHASE chain's table -- a run of controls plus its target -- is one.
+  int lo1[kMaxTables], n1[kMaxTables], lo2[kMaxTables];
   int total;              // total entries
 };
 
-template <typename T>
+__device__ __forceinline__ int diag_index(const DiagArgs &p, int t, uint64_t i) {
+  if (p.lo1[t] >= 0) {
+    const int n1 = p.n1[t], n2 = p.k[t] - n1;
+    const uint64_t a = (i >> p.lo1[t]) & ((1ull << n1) - 1ull);
+    const uint64_t b = (i >> p.lo2[t]) & ((1ull << n2) - 1ull);
+    return (int)(a | (b << n1));
+  }
+  int idx = 0;
+  for (int j = 0; j < p.k[t]; ++j) idx |= (int)((i >> p.qubits[t][j]) & 1ull) << j;
+  return idx;
+}
+
+// Double-float (unevaluated FP32 pairs) complex numbers: on this part FP64
+// runs at 1/64 of the FP32 rate, so the product of an amplitude's table
+// entries is formed in FP32 pairs (~44-bit significand) and only the final
+// multiply of the FP64 amplitude uses the FP64 pipe.
+struct DF2 {
+  float rh, rl, ih, il;
+};
+__device__ __forceinline__ void df_two_sum_fast(float a, float b, float &s, float &e) {
+  s = a + b;
+  e = b - (s - a);
+}
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float &h, float &l) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, fmaf(al, bh, e));
+  df_two_sum_fast(p, e, h, l);
+}
+__device__ __forceinline__ void df_add2(float ah, float al, float bh, float bl, float &h, float &l) {
+  const float s = ah + bh;
+  const float v = s - ah;
+  float e = (ah - (s - v)) + (bh - v);
+  e += al + bl;
+  df_two_sum_fast(s, e, h, l);
+}
+__device__ __forceinline__ DF2 df_cmul(const DF2 &a, const DF2 &b) {
+  float p1h, p1l, p2h, p2l, p3h, p3l, p4h, p4l;
+  df_mul(a.rh, a.rl, b.rh, b.rl, p1h, p1l);
+  df_mul(a.ih, a.il, b.ih, b.il, p2h, p2l);
+  df_mul(a.rh, a.rl, b.ih, b.il, p3h, p3l);
+  df_mul(a.ih, a.il, b.rh, b.rl, p4h, p4l);
+  DF2 r;
+  df_add2(p1h, p1l, -p2h, -p2l, r.rh, r.rl);
+  df_add2(p3h, p3l, p4h, p4l, r.ih, r.il);
+  return r;
+}
+__device__ __forceinline__ DF2 df_from(double2 v) {
+  DF2 r;
+  r.rh = (float)v.x;
+  r.rl = (float)(v.x - (double)r.rh);
+  r.ih = (float)v.y;
+  r.il = (float)(v.y - (double)r.ih);
+  return r;
+}
+
+// FP32 states: tables and products in FP32.  Entries equal to 1 are
+// skipped, and an amplitude whose phase is 1 is neither read nor written.
 __global__ void __launch_bounds__(256)
-    k_diag_tables(typename CT<T>::C *__restrict__ a, uint64_t len,
-                  const typename CT<T>::C *__restrict__ tables,
-                  const __grid_constant__ DiagArgs p) {
-  using C = typename CT<T>::C;
+    k_diag_tables_f32(float2 *__restrict__ a, uint64_t len, const float2 *__restrict__ tables,
+                      const __grid_constant__ DiagArgs p) {
   extern __shared__ unsigned char smem_raw[];
-  C *tab = reinterpret_cast<C *>(smem_raw);
+  float2 *tab = reinterpret_cast<float2 *>(smem_raw);
   for (int j = threadIdx.x; j < p.total; j += blockDim.x) tab[j] = tables[j];
   __syncthreads();
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    C ph = CT<T>::make(1, 0);
+    float2 ph = make_float2(1.f, 0.f);
+    bool unit = true;
     for (int t = 0; t < p.ntables; ++t) {
-      int idx = 0;
-      for (int j = 0; j < p.k[t]; ++j) idx |= (int)((i >> p.qubits[t][j]) & 1ull) << j;
-      C e = tab[p.start[t] + idx];
-      ph = (t == 0) ? e : cmul(ph, e);
+      const float2 e = tab[p.start[t] + diag_index(p, t, i)];
+      if (e.x == 1.f && e.y == 0.f) continue;
+      ph = unit ? e : cmul(ph, e);
+      unit = false;
     }
-    if (ph.x != (T)1 || ph.y != (T)0) a[i] = cmul(a[i], ph);
+    if (!unit && (ph.x != 1.f || ph.y != 0.f)) a[i] = cmul(a[i], ph);
+  }
+}
+
+// FP64 states: the tables are held in shared memory as double-float pairs
+// (converted once per CTA) and multiplied together in FP32 pairs; one FP64
+// complex multiply applies the product.  An amplitude whose entries are all
+// 1 is neither read nor written.
+__global__ void __launch_bounds__(256)
+    k_diag_tables_f64(double2 *__restrict__ a, uint64_t len, const double2 *__restrict__ tables,
+                      const __grid_constant__ DiagArgs p) {
+  extern __shared__ unsigned char smem_raw[];
+  DF2 *tab = reinterpret_cast<DF2 *>(smem_raw);
+  for (int j = threadIdx.x; j < p.total; j += blockDim.x) {
+    const double2 e = tables[j];
+    DF2 d = df_from(e);
+    if (e.x == 1.0 && e.y == 0.0) d.rl = d.il = 0.f;  // exactly (1, 0): the skip test
+    tab[j] = d;
+  }
+  __syncthreads();
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    DF2 ph;
+    int nonunit = 0;
+    for (int t = 0; t < p.ntables; ++t) {
+      const DF2 e = tab[p.start[t] + diag_index(p, t, i)];
+      if (e.rh == 1.f && e.rl == 0.f && e.ih == 0.f && e.il == 0.f) continue;
+      ph = nonunit ? df_cmul(ph, e) : e;
+      ++nonunit;
+    }
+    if (!nonunit) continue;
+    double2 f;
+    if (nonunit == 1) {
+      // a single entry: use its FP64 value exactly
+      int t = 0;
+      for (; t < p.ntables; ++t) {
+        const DF2 e = tab[p.start[t] + diag_index(p, t, i)];
+        if (!(e.rh == 1.f && e.rl == 0.f && e.ih == 0.f && e.il == 0.f)) break;
+      }
+      f = tables[p.start[t] + diag_index(p, t, i)];
+    } else {
+      f = make_double2((double)ph.rh + (double)ph.rl, (double)ph.ih + (double)ph.il);
+    }
+    a[i] = cmul(a[i], f);
   }
 }
 
@@ -219,6 +323,23 @@ static int diag_args(int ntables, const int *ks, const int *qubits, DiagArgs &p)
     qoff += ks[t];
     p.start[t] = total;
     total += 1 << ks[t];
+    // split the (ascending) qubits into contiguous runs; two runs at most
+    // take the shift-and-mask path
+    int runs = 1, n1 = ks[t];
+    for (int j = 1; j < ks[t]; ++j) {
+      if (p.qubits[t][j] <= p.qubits[t][j - 1]) runs = 3;  // not ascending
+      else if (p.qubits[t][j] != p.qubits[t][j - 1] + 1) {
+        if (runs == 1) n1 = j;
+        ++runs;
+      }
+    }
+    if (runs <= 2) {
+      p.lo1[t] = p.qubits[t][0];
+      p.n1[t] = n1;
+      p.lo2[t] = n1 < ks[t] ? p.qubits[t][n1] : 0;
+    } else {
+      p.lo1[t] = -1;
+    }
   }
   p.total = total;
   return total;
@@ -227,9 +348,15 @@ static int diag_args(int ntables, const int *ks, const int *qubits, DiagArgs &p)
 template <typename T>
 static int diag_dev_impl(qvmg_state s, const DiagArgs &p, const void *dtables) {
   using C = typename CT<T>::C;
-  size_t smem = p.total * sizeof(C);
-  k_diag_tables<T><<<grid_for(s->len, 256), 256, smem, s->stream>>>(
-      (C *)s->amps, s->len, (const C *)dtables, p);
+  if constexpr (sizeof(T) == 8) {
+    const size_t smem = p.total * sizeof(DF2);
+    k_diag_tables_f64<<<grid_for(s->len, 256), 256, smem, s->stream>>>(
+        (double2 *)s->amps, s->len, (const double2 *)dtables, p);
+  } else {
+    const size_t smem = p.total * sizeof(C);
+    k_diag_tables_f32<<<grid_for(s->len, 256), 256, smem, s->stream>>>(
+        (float2 *)s->amps, s->len, (const float2 *)dtables, p);
+  }
   QVMG_CHECK_LAUNCH("k_diag_tables");
   return QVMG_OK;
 }
@@ -256,9 +383,9 @@ static bool g_diag_attr_done = false;
 static int diag_attr() {
   if (g_diag_attr_done) return QVMG_OK;
   int bytes = kMaxTables * (1 << kMaxTableBits) * 16;
-  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables<double>,
+  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables_f64,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables<float>,
+  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables_f32,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   g_diag_attr_done = true;
   return QVMG_OK;

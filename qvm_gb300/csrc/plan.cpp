@@ -199,6 +199,9 @@ static void build_tables(const std::vector<const Op *> &diags,
         tq[best].push_back(q);
     members[best].push_back(op);
   }
+  // ascending qubits: a table over a contiguous range of qubits is then
+  // indexed by one shift and mask of the amplitude index
+  for (auto &q : tq) std::sort(q.begin(), q.end());
   tables.resize(tq.size());
   for (size_t t = 0; t < tq.size(); ++t) {
     int kt = (int)tq[t].size();
