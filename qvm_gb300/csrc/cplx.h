@@ -22,6 +22,112 @@ struct CT<float> {
   }
 };
 
+// ---- double-float (FP32 pairs) complex arithmetic ------------------------------
+//
+// On this part the FP64 pipe runs at 1/64 of the FP32 rate.  Fused FP64 tile
+// passes therefore hold their tile as double-float complex numbers (each
+// component an unevaluated sum hi + lo of two floats, ~47 significant bits)
+// and do the arithmetic on the FP32 pipe with error-free transformations
+// (two-sum; two-product through fma), converting from and to the FP64 state
+// at the tile's load and store.  `dfloat` tags that arithmetic; the state in
+// HBM stays complex FP64.
+struct dfloat {};
+struct __align__(16) dfc {
+  float rh, rl, ih, il;
+};
+template <>
+struct CT<dfloat> {
+  using C = dfc;
+};
+
+// float bits -> double bits of the same value (exact for normal floats and
+// zero; float subnormals, below 1.2e-38, come out within 1.2e-38).
+__device__ __forceinline__ unsigned long long df_f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned mag = u & 0x7FFFFFFFu;
+  if (mag == 0) return sign;
+  return sign | (((unsigned long long)mag + (896ull << 23)) << 29);
+}
+__device__ __forceinline__ double df_to_double(float hi, float lo) {
+  return __longlong_as_double(df_f2d_bits(hi)) + __longlong_as_double(df_f2d_bits(lo));
+}
+// x -> (hi, lo): hi is x truncated to 24 bits by integer operations, lo the
+// rounded remainder (one FP64 subtraction, exact, and one conversion).
+// |x| below 2^-126 goes entirely to lo.  |x| must be below 2^128.
+__device__ __forceinline__ void df_split(double x, float &hi, float &lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long mag = u & 0x7FFFFFFFFFFFFFFFull;
+  if (mag < (897ull << 52)) {
+    hi = 0.f;
+    lo = __double2float_rn(x);
+    return;
+  }
+  const unsigned hb = (unsigned)((mag >> 29) - (896ull << 23)) | (unsigned)((u >> 32) & 0x80000000u);
+  hi = __uint_as_float(hb);
+  lo = __double2float_rn(x - __longlong_as_double(df_f2d_bits(hi)));
+}
+__device__ __forceinline__ dfc df_from_double2(double2 v) {
+  dfc r;
+  df_split(v.x, r.rh, r.rl);
+  df_split(v.y, r.ih, r.il);
+  return r;
+}
+// Exact-range conversion for op data (matrices, phase tables).
+__device__ __forceinline__ dfc df_from_double2_any(double2 v) {
+  dfc r;
+  r.rh = __double2float_rn(v.x);
+  r.rl = __double2float_rn(v.x - (double)r.rh);
+  r.ih = __double2float_rn(v.y);
+  r.il = __double2float_rn(v.y - (double)r.ih);
+  return r;
+}
+__device__ __forceinline__ double2 df_to_double2(const dfc &v) {
+  return make_double2(df_to_double(v.rh, v.rl), df_to_double(v.ih, v.il));
+}
+
+// Running double-float sums of complex products: (s, e) per component, s
+// the exact two-sum of the leading product terms, e the low-order terms.
+struct dfacc {
+  float sr, er, si, ei;
+};
+__device__ __forceinline__ void df_acc_term(float &s, float &e, float ah, float al, float bh,
+                                            float bl, bool neg) {
+  float p = ah * bh;
+  float q = fmaf(ah, bh, -p);
+  q = fmaf(ah, bl, q);
+  q = fmaf(al, bh, q);
+  if (neg) {
+    p = -p;
+    q = -q;
+  }
+  const float t = s + p;
+  const float bb = t - s;
+  const float err = (s - (t - bb)) + (p - bb);
+  s = t;
+  e += err + q;
+}
+// acc += a * b
+__device__ __forceinline__ void df_cmac(dfacc &acc, const dfc &a, const dfc &b) {
+  df_acc_term(acc.sr, acc.er, a.rh, a.rl, b.rh, b.rl, false);
+  df_acc_term(acc.sr, acc.er, a.ih, a.il, b.ih, b.il, true);
+  df_acc_term(acc.si, acc.ei, a.rh, a.rl, b.ih, b.il, false);
+  df_acc_term(acc.si, acc.ei, a.ih, a.il, b.rh, b.rl, false);
+}
+__device__ __forceinline__ dfc df_result(const dfacc &acc) {
+  dfc r;
+  r.rh = acc.sr + acc.er;
+  r.rl = acc.er - (r.rh - acc.sr);
+  r.ih = acc.si + acc.ei;
+  r.il = acc.ei - (r.ih - acc.si);
+  return r;
+}
+__device__ __forceinline__ dfc df_cmul(const dfc &a, const dfc &b) {
+  dfacc acc{0.f, 0.f, 0.f, 0.f};
+  df_cmac(acc, a, b);
+  return df_result(acc);
+}
+
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 #include <vector>
 
@@ -502,19 +503,96 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
   if (*abort_flag) ctx.ok = 0;
 }
 
+// ---- double-float ops (fused FP64 tiles) -----------------------------------------
+
+// Element type of the state in HBM: the tile's own type, except for
+// double-float tiles, whose state stays complex FP64.
+template <typename T>
+struct GT {
+  using G = typename CT<T>::C;
+};
+template <>
+struct GT<dfloat> {
+  using G = double2;
+};
+template <typename T>
+constexpr bool kIsDf = std::is_same<T, dfloat>::value;
+
+template <int K, bool S>
+__device__ __forceinline__ void tile_dense_df(dfc *tile, int t, const TileOpDev &op,
+                                              const dfc *mat) {
+  constexpr int D = 1 << K;
+  int sp[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) sp[i] = op.pos[i];
+#pragma unroll
+  for (int i = 1; i < K; ++i)
+#pragma unroll
+    for (int j = i; j > 0; --j)
+      if (sp[j - 1] > sp[j]) {
+        const int x = sp[j];
+        sp[j] = sp[j - 1];
+        sp[j - 1] = x;
+      }
+  unsigned off[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    unsigned o = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if ((c >> j) & 1) o |= 1u << op.pos[j];
+    off[c] = o;
+  }
+  constexpr bool kHoist = K == 1;  // 4 entries in registers; wider ones broadcast from smem
+  dfc mreg[kHoist ? D * D : 1];
+  if constexpr (kHoist) {
+#pragma unroll
+    for (int i = 0; i < D * D; ++i) mreg[i] = mat[i];
+  }
+  const unsigned ngroups = 1u << (t - K);
+  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
+    unsigned b = g;
+#pragma unroll
+    for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
+    dfc v[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = tile[sw<S>(b | off[c])];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      dfacc acc{0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        if constexpr (kHoist) df_cmac(acc, mreg[r * D + c], v[c]);
+        else df_cmac(acc, mat[r * D + c], v[c]);
+      }
+      tile[sw<S>(b | off[r])] = df_result(acc);
+    }
+  }
+}
+
+template <bool S>
+__device__ __forceinline__ void tile_diag_df(dfc *tile, int t, int L,
+                                             const unsigned long long *rowoff, const TileOpDev &op,
+                                             const dfc *table) {
+  const unsigned n = 1u << t;
+  const unsigned rowmask = (1u << L) - 1u;
+  const int k = op.k;
+  for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
+    const unsigned long long g = rowoff[j >> L] | (j & rowmask);
+    int idx = 0;
+    for (int i = 0; i < k; ++i) idx |= (int)((g >> op.pos[i]) & 1ull) << i;
+    const dfc ph = table[idx];
+    if (ph.rh == 1.f && ph.rl == 0.f && ph.ih == 0.f && ph.il == 0.f) continue;
+    const unsigned p = sw<S>(j);
+    tile[p] = df_cmul(tile[p], ph);
+  }
+}
+
 template <typename T, int KMAX, bool S>
 __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
                                         const unsigned long long *rowoff, const TileOpDev &op,
                                         const typename CT<T>::C *md) {
-  if (op.kind == 0) {
-    switch (op.k) {
-      case 1: tile_dense<T, 1, S>(tile, t, op, md); break;
-      case 2: tile_dense<T, 2, S>(tile, t, op, md); break;
-      case 3: if constexpr (KMAX >= 3) tile_dense<T, 3, S>(tile, t, op, md); break;
-      case 4: if constexpr (KMAX >= 4) tile_dense<T, 4, S>(tile, t, op, md); break;
-      case 5: if constexpr (KMAX >= 5) tile_dense<T, 5, S>(tile, t, op, md); break;
-    }
-  } else if (op.kind == 2) {
+  if (op.kind == 2) {
     switch (op.k) {
       case 1: tile_perm<T, 1, S>(tile, t, op); break;
       case 2: tile_perm<T, 2, S>(tile, t, op); break;
@@ -522,8 +600,32 @@ __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
       case 4: if constexpr (KMAX >= 4) tile_perm<T, 4, S>(tile, t, op); break;
       case 5: if constexpr (KMAX >= 5) tile_perm<T, 5, S>(tile, t, op); break;
     }
+    return;
+  }
+  if constexpr (kIsDf<T>) {
+    if (op.kind == 0) {
+      switch (op.k) {
+        case 1: tile_dense_df<1, S>(tile, t, op, md); break;
+        case 2: tile_dense_df<2, S>(tile, t, op, md); break;
+        case 3: if constexpr (KMAX >= 3) tile_dense_df<3, S>(tile, t, op, md); break;
+        case 4: if constexpr (KMAX >= 4) tile_dense_df<4, S>(tile, t, op, md); break;
+        case 5: if constexpr (KMAX >= 5) tile_dense_df<5, S>(tile, t, op, md); break;
+      }
+    } else {
+      tile_diag_df<S>(tile, t, L, rowoff, op, md);
+    }
   } else {
-    tile_diag<T, S>(tile, t, L, rowoff, op, md);
+    if (op.kind == 0) {
+      switch (op.k) {
+        case 1: tile_dense<T, 1, S>(tile, t, op, md); break;
+        case 2: tile_dense<T, 2, S>(tile, t, op, md); break;
+        case 3: if constexpr (KMAX >= 3) tile_dense<T, 3, S>(tile, t, op, md); break;
+        case 4: if constexpr (KMAX >= 4) tile_dense<T, 4, S>(tile, t, op, md); break;
+        case 5: if constexpr (KMAX >= 5) tile_dense<T, 5, S>(tile, t, op, md); break;
+      }
+    } else {
+      tile_diag<T, S>(tile, t, L, rowoff, op, md);
+    }
   }
 }
 
@@ -538,7 +640,7 @@ constexpr int tile_threads() {
 
 template <typename T, int KMAX, int RB>
 __global__ void __launch_bounds__(tile_threads<RB>(), (RB == 5 || RB < 0) ? 2 : (KMAX <= 2 ? 3 : 1))
-    k_tile(typename CT<T>::C *__restrict__ a, const __grid_constant__ TileArgs p) {
+    k_tile(typename GT<T>::G *__restrict__ a, const __grid_constant__ TileArgs p) {
   using C = typename CT<T>::C;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) unsigned long long tc_mbar[2];
@@ -569,8 +671,13 @@ __global__ void __launch_bounds__(tile_threads<RB>(), (RB == 5 || RB < 0) ? 2 : 
   TileOpDev *ops = reinterpret_cast<TileOpDev *>(data + p.ndata);
   TileStageDev *stages = reinterpret_cast<TileStageDev *>(ops + p.nops);
   {
-    const C *gd = reinterpret_cast<const C *>(p.data);
-    for (int i = threadIdx.x; i < p.ndata; i += blockDim.x) data[i] = gd[i];
+    if constexpr (kIsDf<T>) {
+      const double2 *gd = reinterpret_cast<const double2 *>(p.data);
+      for (int i = threadIdx.x; i < p.ndata; i += blockDim.x) data[i] = df_from_double2_any(gd[i]);
+    } else {
+      const C *gd = reinterpret_cast<const C *>(p.data);
+      for (int i = threadIdx.x; i < p.ndata; i += blockDim.x) data[i] = gd[i];
+    }
     const int *gs = reinterpret_cast<const int *>(p.ops);
     int *ss = reinterpret_cast<int *>(ops);
     const int words = p.nops * (int)(sizeof(TileOpDev) / 4);
@@ -610,10 +717,17 @@ __global__ void __launch_bounds__(tile_threads<RB>(), (RB == 5 || RB < 0) ? 2 : 
     __syncthreads();
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
-      const C *src = a + rowoff[el >> L] + (el & rowmask);
+      const typename GT<T>::G *src = a + rowoff[el >> L] + (el & rowmask);
       cp_async16(tile + sw<(RB > 0)>(el), src);
     }
     cp_async_wait_all();
+    if constexpr (kIsDf<T>) {
+      // this thread's own copies have landed: FP64 -> double-float in place
+      for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
+        dfc &d = tile[ch];
+        d = df_from_double2(*reinterpret_cast<const double2 *>(&d));
+      }
+    }
     __syncthreads();
     for (int s = 0; s < p.nstages; ++s) {
       const TileStageDev &st = stages[s];
@@ -645,7 +759,12 @@ __global__ void __launch_bounds__(tile_threads<RB>(), (RB == 5 || RB < 0) ? 2 : 
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
       int4 *dst = reinterpret_cast<int4 *>(a + rowoff[el >> L] + (el & rowmask));
-      __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB > 0)>(el)));
+      if constexpr (kIsDf<T>) {
+        const double2 v = df_to_double2(tile[el]);
+        __stcs(dst, *reinterpret_cast<const int4 *>(&v));
+      } else {
+        __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB > 0)>(el)));
+      }
     }
   }
   if constexpr (RB < 0) {
@@ -712,7 +831,7 @@ static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
   }
   uint64_t grid = std::min<uint64_t>(args.ntiles, (uint64_t)sm_count() * per_sm);
   k_tile<T, KMAX, RB><<<(unsigned)grid, tile_threads<RB>(), smem, s->stream>>>(
-      (typename CT<T>::C *)s->amps, args);
+      (typename GT<T>::G *)s->amps, args);
   QVMG_CHECK_LAUNCH("k_tile");
   return QVMG_OK;
 }
@@ -730,7 +849,7 @@ int launch_tile(qvmg_state s, const TileArgs &args) {
   if (args.kmax < 1 || args.kmax > 5) return fail(QVMG_E_INVALID, "tile op width out of range");
   if (s->prec == QVMG_FP64) {
     if (args.R != 0) return fail(QVMG_E_INVALID, "register stages are FP32 only");
-    return tile_launch_r<double, 0>(s, args, smem);
+    return tile_launch_r<dfloat, 0>(s, args, smem);
   }
   if (args.tc) {
     if (args.R != 0) return fail(QVMG_E_INVALID, "tensor-core passes have no register stages");

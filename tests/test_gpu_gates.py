@@ -251,6 +251,21 @@ def test_small_states_all_paths(gpu, oracle):
                 s.free()
 
 
+def test_fused_fp64_double_float_accuracy(gpu):
+    """Fused FP64 tiles compute in double-float (FP32 pairs); against the
+    plain FP64 kernels at 24 qubits the amplitudes agree to well inside
+    1e-12 and the overlap is 1 to FP64 rounding."""
+    n = 24
+    gs = circuits.random_su_circuit(n, depth=12, seed=6) + circuits.qft(n)
+    plain = _run_program(gs, n, "fp64", False)
+    fused = _run_program(gs, n, "fp64", True, fw=2, tile=12)
+    f, err = plain.fidelity(fused)
+    assert err < 1e-13, err
+    assert f > 1 - 1e-13
+    plain.free()
+    fused.free()
+
+
 def test_determinism_fp64(gpu):
     n = 20
     gs = circuits.random_su_circuit(n, depth=5, seed=8)
