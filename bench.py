@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched QAOA run")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
     ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit FP64 QFT")
+    ap.add_argument("--no-endpoints", action="store_true",
+                    help="skip the server-endpoint and noise measurements")
     ap.add_argument("--no-layers", action="store_true",
                     help="skip the 20-qubit layer circuit with 1000 shots")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -284,6 +286,126 @@ def run_layers_shots(n: int = 20, layers: int = 10, shots: int = 1000, seed: int
             "first_shots": [int(x) for x in out[:4]]}
 
 
+def run_endpoints(n: int = 26, seed: int = 7):
+    """The server endpoints and noise paths on a resident state, each against
+    the reference's own algorithm run on the same GPU where that makes sense:
+    - multishot-measure of 12 qubits x 10^4 trials: one marginal reduction +
+      host replay, against the reference's per-trial reload (device copy) and
+      sequential measure (app/src/api/multishot-measure.lisp:93-109), timed
+      on 100 trials and scaled;
+    - expectation of 8 two-Pauli operators (device copy + program + inner);
+    - wavefunction wire bytes (big-endian, 16 B per amplitude) to the host;
+    - a 4-operator depolarizing Kraus step on one qubit (two passes) against
+      the reference's algorithm (copy, apply K_j, norm, until the sum reaches
+      the draw; src/apply-gate.lisp:16-39), both on the device;
+    - a 10-qubit density matrix (a 20-qubit vector) through a depolarized
+      random circuit."""
+    import random as pyrandom
+
+    from qvm_gb300 import CudaPureState, Program, api, circuits
+    from qvm_gb300.density import DensityQVM
+    from qvm_gb300.noisy import make_pauli_noise_map
+
+    out = {"qubits": n, "precision": "fp64"}
+    gs = circuits.random_su_circuit(n, depth=6, seed=seed)
+    prep = Program()
+    prep.add_gates(gs)
+    prep.plan(n, "fp64", fused=True, fusion_width=2)
+    s = CudaPureState(n, "fp64")
+    prep.run(s, fused=True)
+    s.sync()
+
+    def timed(fn, reps=3):
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            r = fn()
+            best = min(best, time.perf_counter() - t0)
+        return best, r
+
+    # multishot-measure: 12 qubits, 10^4 trials
+    qubits = list(range(0, n, 2))[:12]
+    rng = pyrandom.Random(seed)
+    t_ours, bits = timed(lambda: api.measure_trials(s, qubits, 10000, rng))
+    work = CudaPureState(n, "fp64")
+
+    def per_trial(trials):
+        r = pyrandom.Random(seed)
+        for _ in range(trials):
+            work.copy_from(s)
+            for q in qubits:
+                work.measure(q, r.random())
+        work.sync()
+    t_ref100, _ = timed(lambda: per_trial(100), reps=1)
+    out["multishot_measure"] = {"measured_qubits": len(qubits), "trials": 10000,
+                                "ms": 1e3 * t_ours, "trials_per_s": 10000 / t_ours,
+                                "per_trial_reload_ms_est": 1e3 * t_ref100 * 100,
+                                "speedup": t_ref100 * 100 / t_ours}
+    # expectation of 8 operators
+    ops = [f"Z {a}\nZ {a + 1}" for a in range(0, 16, 2)]
+    prep_quil = "\n".join(f"RY({0.1 * (q + 1)}) {q}" for q in range(n)) + "\nCNOT 0 1\nCNOT 2 3"
+    t_exp, vals = timed(lambda: api.perform_expectation(prep_quil, ops, n), reps=2)
+    out["expectation"] = {"operators": len(ops), "ms": 1e3 * t_exp,
+                          "ms_per_operator_incl_prep": 1e3 * t_exp / len(ops)}
+    # wire bytes
+    t_wire, raw = timed(lambda: s.wavefunction_octets(), reps=2)
+    out["wavefunction_octets"] = {"bytes": len(raw), "ms": 1e3 * t_wire,
+                                  "GB_per_s": len(raw) / t_wire / 1e9}
+    del raw
+    # Kraus step vs the reference algorithm on the device
+    kraus = make_pauli_noise_map(0.05, 0.05, 0.05)
+    q0 = [3]
+
+    def ours():
+        s.apply_kraus(kraus, q0, 0.99)   # a late draw: every p_j is needed
+        s.sync()
+    t_k, _ = timed(ours)
+    trial = CudaPureState(n, "fp64")
+
+    def reference_algorithm():
+        summed = 0.0
+        for k in kraus:
+            trial.copy_from(s)
+            trial.apply_matrix(k, q0)
+            summed += trial.norm() ** 2
+            if summed >= 0.99:
+                break
+        trial.normalize()
+        trial.sync()
+    t_r, _ = timed(reference_algorithm)
+    hmat = np.array([[1, 1], [1, -1]], dtype=np.complex128) / np.sqrt(2)
+    t_gate, _ = timed(lambda: (s.apply_matrix(hmat, q0), s.sync()))
+    out["kraus_step"] = {"operators": len(kraus), "ms": 1e3 * t_k,
+                         "reference_algorithm_ms": 1e3 * t_r, "speedup": t_r / t_k,
+                         "plain_gate_ms": 1e3 * t_gate}
+    trial.free()
+    work.free()
+    s.free()
+    prep.free()
+    # noisy density matrix: 10 qubits (20-qubit vector), depolarizing 1q noise on every H
+    nd = 10
+    dq = DensityQVM(nd, fused=True, fusion_width=4)
+    for q in range(nd):
+        dq.set_noisy_gate("H", [q], [k @ hmat for k in make_pauli_noise_map(0.01, 0.01, 0.01)])
+    prog = "\n".join(f"H {q}" for q in range(nd)) + "\n" + "\n".join(
+        f"CNOT {q} {q + 1}\nRZ({0.3 * q}) {q + 1}" for q in range(nd - 1))
+    dq.load_program(prog)
+    dq.run()
+    dq.state.sync()
+
+    def dens():
+        dq.reset_quantum_state()
+        dq.run()
+        dq.state.sync()
+    t_d, _ = timed(dens)
+    ngates = nd + 2 * (nd - 1)
+    out["density_matrix"] = {"qubits": nd, "vector_qubits": 2 * nd, "gates": ngates,
+                             "ms": 1e3 * t_d, "gates_per_s": ngates / t_d,
+                             "trace": float(np.sum(dq.probabilities()))}
+    dq.free()
+    return out
+
+
 def run_serving(arrive_s: float = 1.5, drain_s: float = 60.0, seed: int = 5):
     """Serving stream: Poisson arrivals (mean 200/s) of random-layer, QFT and
     QAOA programs with 10..30 qubits, depth 5..40, shots 1..1e4, FP32 or FP64,
@@ -501,6 +623,8 @@ def main():
         result["qft28_fp64"] = run_qft_fp64()
     if not args.no_layers and rank == 0:
         result["layers20_shots"] = run_layers_shots()
+    if not args.no_endpoints and rank == 0:
+        result["endpoints"] = run_endpoints()
     if not args.no_batch and rank == 0:
         result["batch_qaoa"] = run_qaoa_batch()
     if not args.no_serve and rank == 0:

@@ -73,13 +73,13 @@ def perform_probabilities(quil, num_qubits: int, **qvm_kw):
     return qvm, qvm.state.probabilities()
 
 
-def wavefunction_octets(qvm_or_state) -> bytes:
+def wavefunction_octets(qvm_or_state) -> memoryview:
     """The wavefunction endpoint's reply body: 16 octets per amplitude."""
     s = qvm_or_state.state if isinstance(qvm_or_state, PureStateQVM) else qvm_or_state
     return s.wavefunction_octets()
 
 
-def probabilities_octets(qvm_or_state) -> bytes:
+def probabilities_octets(qvm_or_state) -> memoryview:
     """The probabilities endpoint's reply body: 8 octets per probability."""
     s = qvm_or_state.state if isinstance(qvm_or_state, PureStateQVM) else qvm_or_state
     return s.probabilities_octets()

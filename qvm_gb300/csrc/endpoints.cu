@@ -244,37 +244,33 @@ __global__ void k_wire_probs(const C *__restrict__ a, unsigned long long *__rest
     out[i] = bswap64(prob_f64(a[i]));  // the values qvmg_probabilities returns
 }
 
+static int produce_wire(qvmg_state s, uint64_t off, uint64_t n, void *dst, void *ctx) {
+  const int probs = *static_cast<const int *>(ctx);
+  const int grid = grid_for(n, 256);
+  if (probs) {
+    if (s->prec == QVMG_FP64)
+      k_wire_probs<double2><<<grid, 256, 0, s->stream>>>((const double2 *)s->amps + off,
+                                                          (unsigned long long *)dst, n);
+    else
+      k_wire_probs<float2><<<grid, 256, 0, s->stream>>>((const float2 *)s->amps + off,
+                                                         (unsigned long long *)dst, n);
+  } else {
+    if (s->prec == QVMG_FP64)
+      k_wire_amps<double2><<<grid, 256, 0, s->stream>>>((const double2 *)s->amps + off,
+                                                         (ulonglong2 *)dst, n);
+    else
+      k_wire_amps<float2><<<grid, 256, 0, s->stream>>>((const float2 *)s->amps + off,
+                                                        (ulonglong2 *)dst, n);
+  }
+  QVMG_CHECK_LAUNCH("k_wire");
+  return QVMG_OK;
+}
+
 static int wire_stream(qvmg_state s, uint8_t *out, int probs) {
   int rc = check_state(s);
   if (rc) return rc;
   if (!out) return fail(QVMG_E_INVALID, "null output");
-  const uint64_t per = probs ? 8 : 16;
-  const uint64_t chunk = std::min<uint64_t>(s->len, 1ull << 22);
-  if ((rc = ensure_staging(s, chunk * per))) return rc;
-  for (uint64_t off = 0; off < s->len; off += chunk) {
-    const uint64_t n = std::min(chunk, s->len - off);
-    const int grid = grid_for(n, 256);
-    if (probs) {
-      if (s->prec == QVMG_FP64)
-        k_wire_probs<double2><<<grid, 256, 0, s->stream>>>((const double2 *)s->amps + off,
-                                                            (unsigned long long *)s->staging, n);
-      else
-        k_wire_probs<float2><<<grid, 256, 0, s->stream>>>((const float2 *)s->amps + off,
-                                                           (unsigned long long *)s->staging, n);
-    } else {
-      if (s->prec == QVMG_FP64)
-        k_wire_amps<double2><<<grid, 256, 0, s->stream>>>((const double2 *)s->amps + off,
-                                                           (ulonglong2 *)s->staging, n);
-      else
-        k_wire_amps<float2><<<grid, 256, 0, s->stream>>>((const float2 *)s->amps + off,
-                                                          (ulonglong2 *)s->staging, n);
-    }
-    QVMG_CHECK_LAUNCH("k_wire");
-    QVMG_CUDA(cudaMemcpyAsync(out + off * per, s->staging, n * per, cudaMemcpyDeviceToHost,
-                              s->stream));
-    QVMG_CUDA(cudaStreamSynchronize(s->stream));
-  }
-  return QVMG_OK;
+  return stream_to_host(s, s->len, probs ? 8 : 16, out, produce_wire, &probs);
 }
 
 }  // namespace qvmg

@@ -121,49 +121,9 @@ __device__ __forceinline__ int diag_index(const DiagArgs &p, int t, uint64_t i) 
   return idx;
 }
 
-// Double-float (unevaluated FP32 pairs) complex numbers: on this part FP64
-// runs at 1/64 of the FP32 rate, so the product of an amplitude's table
-// entries is formed in FP32 pairs (~44-bit significand) and only the final
-// multiply of the FP64 amplitude uses the FP64 pipe.
-struct DF2 {
-  float rh, rl, ih, il;
-};
-__device__ __forceinline__ void df_two_sum_fast(float a, float b, float &s, float &e) {
-  s = a + b;
-  e = b - (s - a);
-}
-__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float &h, float &l) {
-  const float p = ah * bh;
-  float e = fmaf(ah, bh, -p);
-  e = fmaf(ah, bl, fmaf(al, bh, e));
-  df_two_sum_fast(p, e, h, l);
-}
-__device__ __forceinline__ void df_add2(float ah, float al, float bh, float bl, float &h, float &l) {
-  const float s = ah + bh;
-  const float v = s - ah;
-  float e = (ah - (s - v)) + (bh - v);
-  e += al + bl;
-  df_two_sum_fast(s, e, h, l);
-}
-__device__ __forceinline__ DF2 df_cmul(const DF2 &a, const DF2 &b) {
-  float p1h, p1l, p2h, p2l, p3h, p3l, p4h, p4l;
-  df_mul(a.rh, a.rl, b.rh, b.rl, p1h, p1l);
-  df_mul(a.ih, a.il, b.ih, b.il, p2h, p2l);
-  df_mul(a.rh, a.rl, b.ih, b.il, p3h, p3l);
-  df_mul(a.ih, a.il, b.rh, b.rl, p4h, p4l);
-  DF2 r;
-  df_add2(p1h, p1l, -p2h, -p2l, r.rh, r.rl);
-  df_add2(p3h, p3l, p4h, p4l, r.ih, r.il);
-  return r;
-}
-__device__ __forceinline__ DF2 df_from(double2 v) {
-  DF2 r;
-  r.rh = (float)v.x;
-  r.rl = (float)(v.x - (double)r.rh);
-  r.ih = (float)v.y;
-  r.il = (float)(v.y - (double)r.ih);
-  return r;
-}
+// The product of an amplitude's table entries is formed in double-float
+// (dfc, cplx.h: FP32 pairs, ~47-bit significand) on the FP32 pipe; on this
+// part the FP64 pipe runs at 1/64 of the FP32 rate.
 
 // FP32 states: tables and products in FP32.  Entries equal to 1 are
 // skipped, and an amplitude whose phase is 1 is neither read nor written.
@@ -196,20 +156,20 @@ __global__ void __launch_bounds__(256)
     k_diag_tables_f64(double2 *__restrict__ a, uint64_t len, const double2 *__restrict__ tables,
                       const __grid_constant__ DiagArgs p) {
   extern __shared__ unsigned char smem_raw[];
-  DF2 *tab = reinterpret_cast<DF2 *>(smem_raw);
+  dfc *tab = reinterpret_cast<dfc *>(smem_raw);
   for (int j = threadIdx.x; j < p.total; j += blockDim.x) {
     const double2 e = tables[j];
-    DF2 d = df_from(e);
+    dfc d = df_from_double2_any(e);
     if (e.x == 1.0 && e.y == 0.0) d.rl = d.il = 0.f;  // exactly (1, 0): the skip test
     tab[j] = d;
   }
   __syncthreads();
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    DF2 ph;
+    dfc ph;
     int nonunit = 0;
     for (int t = 0; t < p.ntables; ++t) {
-      const DF2 e = tab[p.start[t] + diag_index(p, t, i)];
+      const dfc e = tab[p.start[t] + diag_index(p, t, i)];
       if (e.rh == 1.f && e.rl == 0.f && e.ih == 0.f && e.il == 0.f) continue;
       ph = nonunit ? df_cmul(ph, e) : e;
       ++nonunit;
@@ -220,12 +180,13 @@ __global__ void __launch_bounds__(256)
       // a single entry: use its FP64 value exactly
       int t = 0;
       for (; t < p.ntables; ++t) {
-        const DF2 e = tab[p.start[t] + diag_index(p, t, i)];
+        const dfc e = tab[p.start[t] + diag_index(p, t, i)];
         if (!(e.rh == 1.f && e.rl == 0.f && e.ih == 0.f && e.il == 0.f)) break;
       }
       f = tables[p.start[t] + diag_index(p, t, i)];
     } else {
-      f = make_double2((double)ph.rh + (double)ph.rl, (double)ph.ih + (double)ph.il);
+      // float -> double by integer bit moves: only the two adds use the FP64 pipe
+      f = make_double2(df_to_double(ph.rh, ph.rl), df_to_double(ph.ih, ph.il));
     }
     a[i] = cmul(a[i], f);
   }
@@ -349,7 +310,7 @@ template <typename T>
 static int diag_dev_impl(qvmg_state s, const DiagArgs &p, const void *dtables) {
   using C = typename CT<T>::C;
   if constexpr (sizeof(T) == 8) {
-    const size_t smem = p.total * sizeof(DF2);
+    const size_t smem = p.total * sizeof(dfc);
     k_diag_tables_f64<<<grid_for(s->len, 256), 256, smem, s->stream>>>(
         (double2 *)s->amps, s->len, (const double2 *)dtables, p);
   } else {

@@ -66,6 +66,7 @@ struct qvmg_state_s {
   uint64_t staging_bytes = 0;
   void *pinned = nullptr;          // pinned host bounce buffer
   uint64_t pinned_bytes = 0;
+  cudaEvent_t xfer_ev[2] = {nullptr, nullptr};  // pipelined device -> host transfers
   double *dvec = nullptr;          // device vector for draws / op tables
   uint64_t dvec_bytes = 0;
 };
@@ -82,6 +83,16 @@ int sm_count();
 int ensure_dvec(qvmg_state s, uint64_t bytes);
 int ensure_staging(qvmg_state s, uint64_t bytes);
 int ensure_pinned(qvmg_state s, uint64_t bytes);
+
+// Pipelined device -> host transfer of `count` elements of `elem` bytes into
+// `out`: chunk by chunk, produce(off, n, dst) queues on the state's stream
+// the device work that writes elements [off, off+n) into device memory
+// `dst` (the state's staging), or, when `produce` is null, the elements are
+// the state's own amplitudes.  Chunks go through two pinned buffers; host
+// threads copy chunk i-1 to `out` while chunk i is produced and copied.
+using ProduceFn = int (*)(qvmg_state s, uint64_t off, uint64_t n, void *dst, void *ctx);
+int stream_to_host(qvmg_state s, uint64_t count, size_t elem, void *out, ProduceFn produce,
+                   void *ctx);
 
 // Validation helpers.
 int check_state(qvmg_state s);

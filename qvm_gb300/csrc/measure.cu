@@ -582,25 +582,22 @@ int qvmg_sample(qvmg_state s, const double *draws, uint64_t nshots, int rule, ui
   return QVMG_OK;
 }
 
+static int produce_probs(qvmg_state s, uint64_t off, uint64_t n, void *dst, void *) {
+  if (s->prec == QVMG_FP64)
+    k_probs<double><<<grid_for(n, 256), 256, 0, s->stream>>>((const double2 *)s->amps + off,
+                                                             (double *)dst, n);
+  else
+    k_probs<float><<<grid_for(n, 256), 256, 0, s->stream>>>((const float2 *)s->amps + off,
+                                                            (double *)dst, n);
+  QVMG_CHECK_LAUNCH("k_probs");
+  return QVMG_OK;
+}
+
 int qvmg_probabilities(qvmg_state s, double *out) {
   int rc = check_state(s);
   if (rc) return rc;
   if (!out) return fail(QVMG_E_INVALID, "null output");
-  const uint64_t chunk = std::min<uint64_t>(s->len, 1ull << 22);
-  if ((rc = ensure_staging(s, chunk * 8))) return rc;
-  for (uint64_t off = 0; off < s->len; off += chunk) {
-    uint64_t n = std::min(chunk, s->len - off);
-    if (s->prec == QVMG_FP64)
-      k_probs<double><<<grid_for(n, 256), 256, 0, s->stream>>>(
-          (const double2 *)s->amps + off, (double *)s->staging, n);
-    else
-      k_probs<float><<<grid_for(n, 256), 256, 0, s->stream>>>(
-          (const float2 *)s->amps + off, (double *)s->staging, n);
-    QVMG_CHECK_LAUNCH("k_probs");
-    QVMG_CUDA(cudaMemcpyAsync(out + off, s->staging, n * 8, cudaMemcpyDeviceToHost, s->stream));
-    QVMG_CUDA(cudaStreamSynchronize(s->stream));
-  }
-  return QVMG_OK;
+  return stream_to_host(s, s->len, 8, out, produce_probs, nullptr);
 }
 
 int qvmg_norm(qvmg_state s, double *norm) {

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <thread>
 #include <mutex>
 #include <string>
 
@@ -156,6 +157,70 @@ static int order_after(qvmg_state waiter, qvmg_state producer) {
 
 int order_states(qvmg_state waiter, qvmg_state producer) { return order_after(waiter, producer); }
 
+// Host copy of one chunk from pinned memory, split over a few threads
+// (large chunks are bound by a single core's copy rate).
+static void parallel_copy(void *dst, const void *src, size_t bytes) {
+  const size_t kMinPerThread = 4u << 20;
+  int nt = (int)std::min<size_t>(8, bytes / kMinPerThread);
+  if (nt <= 1) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  std::vector<std::thread> th;
+  const size_t part = (bytes / nt + 63) & ~(size_t)63;
+  for (int i = 0; i < nt; ++i) {
+    const size_t b0 = (size_t)i * part;
+    if (b0 >= bytes) break;
+    const size_t len = std::min(part, bytes - b0);
+    th.emplace_back([=] { std::memcpy((char *)dst + b0, (const char *)src + b0, len); });
+  }
+  for (auto &t : th) t.join();
+}
+
+int stream_to_host(qvmg_state s, uint64_t count, size_t elem, void *out, ProduceFn produce,
+                   void *ctx) {
+  const uint64_t chunk = std::min<uint64_t>(count, (64ull << 20) / elem);
+  const size_t cb = (size_t)chunk * elem;
+  int rc;
+  if (produce && (rc = ensure_staging(s, 2 * cb))) return rc;
+  if ((rc = ensure_pinned(s, 2 * cb))) return rc;
+  for (auto &e : s->xfer_ev)
+    if (!e) QVMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  const uint64_t nchunks = (count + chunk - 1) / chunk;
+  for (uint64_t i = 0; i <= nchunks; ++i) {
+    if (i < nchunks) {
+      const int b = (int)(i & 1);
+      const uint64_t off = i * chunk, n = std::min(chunk, count - off);
+      const void *src;
+      if (produce) {
+        void *dst = (char *)s->staging + b * cb;
+        if ((rc = produce(s, off, n, dst, ctx))) return rc;
+        src = dst;
+      } else {
+        src = (const char *)s->amps + off * elem;
+      }
+      QVMG_CUDA(cudaMemcpyAsync((char *)s->pinned + b * cb, src, n * elem, cudaMemcpyDeviceToHost,
+                                s->stream));
+      QVMG_CUDA(cudaEventRecord(s->xfer_ev[b], s->stream));
+    }
+    if (i >= 1) {
+      const uint64_t j = i - 1;
+      const int b = (int)(j & 1);
+      const uint64_t off = j * chunk, n = std::min(chunk, count - off);
+      QVMG_CUDA(cudaEventSynchronize(s->xfer_ev[b]));
+      parallel_copy((char *)out + off * elem, (const char *)s->pinned + b * cb, n * elem);
+    }
+  }
+  return QVMG_OK;
+}
+
+static int produce_f64_from_f32(qvmg_state s, uint64_t off, uint64_t n, void *dst, void *) {
+  k_f32_to_f64<<<grid_for(n, 256), 256, 0, s->stream>>>((const float2 *)s->amps + off,
+                                                        (double2 *)dst, n);
+  QVMG_CHECK_LAUNCH("k_f32_to_f64");
+  return QVMG_OK;
+}
+
 }  // namespace qvmg
 
 using namespace qvmg;
@@ -247,6 +312,8 @@ int qvmg_state_free(qvmg_state s) {
   if (s->hres) cudaFreeHost(s->hres);
   if (s->staging) cudaFree(s->staging);
   if (s->pinned) cudaFreeHost(s->pinned);
+  for (auto &e : s->xfer_ev)
+    if (e) cudaEventDestroy(e);
   if (s->dvec) cudaFree(s->dvec);
   if (s->stream) cudaStreamDestroy(s->stream);
   s->amps = nullptr;
@@ -301,23 +368,8 @@ int qvmg_state_download(qvmg_state s, double *amps) {
   int rc = check_state(s);
   if (rc) return rc;
   if (!amps) return fail(QVMG_E_INVALID, "null host buffer");
-  if (s->prec == QVMG_FP64) {
-    QVMG_CUDA(cudaMemcpyAsync(amps, s->amps, s->len * 16, cudaMemcpyDeviceToHost, s->stream));
-    QVMG_CUDA(cudaStreamSynchronize(s->stream));
-    return QVMG_OK;
-  }
-  uint64_t chunk = std::min(kChunk, s->len);
-  if ((rc = ensure_staging(s, chunk * 16))) return rc;
-  for (uint64_t off = 0; off < s->len; off += chunk) {
-    uint64_t n = std::min(chunk, s->len - off);
-    k_f32_to_f64<<<grid_for(n, 256), 256, 0, s->stream>>>((const float2 *)s->amps + off,
-                                                          (double2 *)s->staging, n);
-    QVMG_CHECK_LAUNCH("k_f32_to_f64");
-    QVMG_CUDA(cudaMemcpyAsync(amps + 2 * off, s->staging, n * 16, cudaMemcpyDeviceToHost,
-                              s->stream));
-    QVMG_CUDA(cudaStreamSynchronize(s->stream));
-  }
-  return QVMG_OK;
+  return stream_to_host(s, s->len, 16, amps,
+                        s->prec == QVMG_FP64 ? nullptr : produce_f64_from_f32, nullptr);
 }
 
 int qvmg_state_copy(qvmg_state dst, qvmg_state src) {

@@ -209,17 +209,18 @@ class CudaPureState:
                ctypes.byref(used))
         return bits, int(used.value)
 
-    def wavefunction_octets(self) -> bytes:
-        """The amplitudes as big-endian complex doubles (16 octets each)."""
+    def wavefunction_octets(self) -> memoryview:
+        """The amplitudes as big-endian complex doubles (16 octets each), as a
+        bytes-like view of the host buffer they were written into."""
         out = np.empty(16 << self._n, dtype=np.uint8)
         L.call("qvmg_wavefunction_octets", self.handle, out.ctypes.data_as(ctypes.c_void_p))
-        return out.tobytes()
+        return memoryview(out)
 
-    def probabilities_octets(self) -> bytes:
-        """|a_i|^2 as big-endian doubles (8 octets each)."""
+    def probabilities_octets(self) -> memoryview:
+        """|a_i|^2 as big-endian doubles (8 octets each), bytes-like."""
         out = np.empty(8 << self._n, dtype=np.uint8)
         L.call("qvmg_probabilities_octets", self.handle, out.ctypes.data_as(ctypes.c_void_p))
-        return out.tobytes()
+        return memoryview(out)
 
     def norm(self) -> float:
         n = ctypes.c_double()
