@@ -416,15 +416,15 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
   A.subs = b->subs;
   A.expect = b->expect;
   A.counter = b->counter;
-  static bool attr = false;
-  if (!attr) {
-    int bytes = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges + 16;
-    e = cudaFuncSetAttribute(k_qaoa_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess) {
-      qaoa_release(b);
-      return cuda_fail(e, "cudaFuncSetAttribute(k_qaoa_batch)");
-    }
-    attr = true;
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  e = once(attr_once, attr_err, [] {
+    const int bytes = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges + 16;
+    return cudaFuncSetAttribute(k_qaoa_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  });
+  if (e != cudaSuccess) {
+    qaoa_release(b);
+    return cuda_fail(e, "cudaFuncSetAttribute(k_qaoa_batch)");
   }
   *out = b;
   return QVMG_OK;

@@ -184,18 +184,17 @@ static int marginal_device(qvmg_state s, int k, const int *qubits, double **dout
   double *partial = (double *)s->staging;
   double *out = partial + npartial;
   const size_t smem = kMarginalWarps * nb * sizeof(double);
-  static std::once_flag attr;
-  cudaError_t attr_err = cudaSuccess;
-  std::call_once(attr, [&] {
-    attr_err = cudaFuncSetAttribute(k_marginal<double2>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kMarginalWarps * (1 << kMarginalLocalMax) * 8);
-    if (attr_err == cudaSuccess)
-      attr_err = cudaFuncSetAttribute(k_marginal<float2>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kMarginalWarps * (1 << kMarginalLocalMax) * 8);
-  });
-  QVMG_CUDA(attr_err);
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  QVMG_CUDA(once(attr_once, attr_err, [] {
+    const int bytes = kMarginalWarps * (1 << kMarginalLocalMax) * 8;
+    cudaError_t e =
+        cudaFuncSetAttribute(k_marginal<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_marginal<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               bytes);
+    return e;
+  }));
   const unsigned grid = (unsigned)(groups * C);
   if (s->prec == QVMG_FP64)
     k_marginal<double2><<<grid, kMarginalThreads, smem, s->stream>>>((const double2 *)s->amps, p,

@@ -340,15 +340,18 @@ static int diag_tables_impl(qvmg_state s, int ntables, const int *ks, const int 
 }
 
 // Attribute setup for the large-smem diagonal kernel.
-static bool g_diag_attr_done = false;
 static int diag_attr() {
-  if (g_diag_attr_done) return QVMG_OK;
-  int bytes = kMaxTables * (1 << kMaxTableBits) * 16;
-  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables_f64,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  QVMG_CUDA(cudaFuncSetAttribute(k_diag_tables_f32,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  g_diag_attr_done = true;
+  static std::once_flag flag;
+  static cudaError_t err = cudaSuccess;
+  QVMG_CUDA(once(flag, err, [] {
+    const int bytes = kMaxTables * (1 << kMaxTableBits) * 16;
+    cudaError_t e = cudaFuncSetAttribute(k_diag_tables_f64,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_diag_tables_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               bytes);
+    return e;
+  }));
   return QVMG_OK;
 }
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -93,6 +94,15 @@ int ensure_pinned(qvmg_state s, uint64_t bytes);
 using ProduceFn = int (*)(qvmg_state s, uint64_t off, uint64_t n, void *dst, void *ctx);
 int stream_to_host(qvmg_state s, uint64_t count, size_t elem, void *out, ProduceFn produce,
                    void *ctx);
+
+// One-time process-wide setup (kernel attributes and the like), safe when
+// several threads make their first call at once: `setup` runs exactly once
+// and every caller gets its result.
+template <typename F>
+cudaError_t once(std::once_flag &flag, cudaError_t &result, F &&setup) {
+  std::call_once(flag, [&] { result = setup(); });
+  return result;
+}
 
 // Validation helpers.
 int check_state(qvmg_state s);

@@ -793,17 +793,18 @@ size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages)
 
 template <typename T, int KMAX, int RB>
 static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
-  static bool attr = false;  // per instantiation
-  if (!attr) {
-    QVMG_CUDA(cudaFuncSetAttribute(k_tile<T, KMAX, RB>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kTileMaxSmem));
+  static std::once_flag attr_once;  // per instantiation
+  static cudaError_t attr_err = cudaSuccess;
+  QVMG_CUDA(once(attr_once, attr_err, [] {
+    cudaError_t e = cudaFuncSetAttribute(k_tile<T, KMAX, RB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kTileMaxSmem);
     // the whole unified L1/shared array as shared memory: the occupancy
     // query (and the launch) then fit as many tiles per SM as the bytes allow
-    QVMG_CUDA(cudaFuncSetAttribute(k_tile<T, KMAX, RB>,
-                                   cudaFuncAttributePreferredSharedMemoryCarveout,
-                                   cudaSharedmemCarveoutMaxShared));
-    attr = true;
-  }
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tile<T, KMAX, RB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    return e;
+  }));
   // Persistent grid: as many CTAs as fit on every SM at once (registers and
   // shared memory), each looping over tiles.
   int per_sm = 0;
@@ -816,15 +817,21 @@ static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
     // 1 KiB the runtime reserves per CTA), registers, and the 512 TMEM
     // columns of an SM.  (The persistent loop is correct for any grid.)
     static int smem_sm = 0, regs = 0, stat = 0;
-    if (!smem_sm) {
+    static std::once_flag info_once;
+    static cudaError_t info_err = cudaSuccess;
+    QVMG_CUDA(once(info_once, info_err, [] {
       int dev = 0;
-      QVMG_CUDA(cudaGetDevice(&dev));
-      QVMG_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
       cudaFuncAttributes fa;
-      QVMG_CUDA(cudaFuncGetAttributes(&fa, k_tile<T, KMAX, RB>));
-      regs = fa.numRegs;
-      stat = (int)fa.sharedSizeBytes;
-    }
+      if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_tile<T, KMAX, RB>);
+      if (e == cudaSuccess) {
+        regs = fa.numRegs;
+        stat = (int)fa.sharedSizeBytes;
+      }
+      return e;
+    }));
     const int by_smem = smem_sm / (int)(smem + (size_t)stat + 1024);
     const int by_regs = 65536 / (((regs * 32 + 255) / 256) * 256 * (tile_threads<RB>() / 32));
     per_sm = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTcCols));
