@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched QAOA run")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
     ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit FP64 QFT")
+    ap.add_argument("--no-32q", action="store_true", help="skip the 32-qubit random circuit")
     ap.add_argument("--no-endpoints", action="store_true",
                     help="skip the server-endpoint and noise measurements")
     ap.add_argument("--no-layers", action="store_true",
@@ -406,6 +407,61 @@ def run_endpoints(n: int = 26, seed: int = 7):
     return out
 
 
+def run_random32(fw: int, tile: int, engine: str, shots: int = 4096, seed: int = 3,
+                 runs: int = 3):
+    """The random circuit at 32 qubits (depth 20, 960 gates): fused FP32
+    (32 GiB state) with the tuned engine and with the tensor-core engine,
+    against fused FP64 (64 GiB state; double-float tiles, within 1e-13 of the
+    plain FP64 kernels).  The plain FP64 kernels would take ~80 s here and
+    are timed at 30 qubits instead.  Fidelity, max amplitude error and the
+    shots drawn from the same uniforms are reported."""
+    from qvm_gb300 import CudaPureState, Program, circuits
+    from qvm_gb300.autotune import apply_engine
+    n = 32
+    gates = circuits.random_su_circuit(n, depth=20, seed=seed)
+    G = len(gates)
+    s32 = CudaPureState(n, "fp32")
+    out = {"workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth 20, {G} gates"}
+    for label, (f, t, e) in (("fp32_" + engine, (fw, tile, engine)), ("fp32_tc", (4, 13, "tc"))):
+        prog = Program()
+        prog.add_gates(gates)
+        apply_engine(prog, e)
+        prog.plan(n, "fp32", fused=True, fusion_width=f, tile_qubits=t)
+        best = float("inf")
+        for _ in range(runs + 1):
+            s32.set_to_zero_state()
+            ms, _ = prog.run_profiled(s32, fused=True)
+            best = min(best, float(ms.sum()))
+        out[label] = {"ms": best, "gates_per_s": G / (best / 1e3), "fusion_width": f,
+                      "tile_qubits": t}
+        prog.free()
+    s64 = CudaPureState(n, "fp64")
+    prog = Program()
+    prog.add_gates(gates)
+    prog.plan(n, "fp64", fused=True, fusion_width=2, tile_qubits=12)
+    t0 = time.perf_counter()
+    prog.run(s64, fused=True)
+    s64.sync()
+    out["fp64_fused_ms"] = 1e3 * (time.perf_counter() - t0)
+    prog.free()
+    # the state of the tuned FP32 engine against it
+    prog = Program()
+    prog.add_gates(gates)
+    apply_engine(prog, engine)
+    prog.plan(n, "fp32", fused=True, fusion_width=fw, tile_qubits=tile)
+    s32.set_to_zero_state()
+    prog.run(s32, fused=True)
+    f, err = s64.fidelity(s32)
+    draws = np.random.default_rng(seed + 1).random(shots)
+    same = int((s64.sample(draws) == s32.sample(draws)).sum())
+    out["fidelity"] = {"fused_fp32_vs_fp64": f, "max_abs_err": err, "shots": shots,
+                       "identical_shots": same}
+    prog.free()
+    s64.free()
+    s32.free()
+    return out
+
+
 def run_serving(arrive_s: float = 1.5, drain_s: float = 60.0, seed: int = 5):
     """Serving stream: Poisson arrivals (mean 200/s) of random-layer, QFT and
     QAOA programs with 10..30 qubits, depth 5..40, shots 1..1e4, FP32 or FP64,
@@ -619,6 +675,10 @@ def main():
                               "shots": int(args.shots),
                               "identical_shots": int((sh64 == sh32).sum())}
         s64.free()
+    if not args.no_32q and rank == 0:
+        s32.free()  # 8 GiB back before the 32 + 64 GiB states
+        result["random32"] = run_random32(args.fw, args.tile, args.engine)
+        s32 = CudaPureState(n, "fp32")
     if not args.no_qft and rank == 0:
         result["qft28_fp64"] = run_qft_fp64()
     if not args.no_layers and rank == 0:
