@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched QAOA run")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
     ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit FP64 QFT")
+    ap.add_argument("--qft-n", type=int, default=28,
+                    help="qubits of the FP64 QFT leg (smaller for profiling)")
     ap.add_argument("--no-32q", action="store_true", help="skip the 32-qubit random circuit")
     ap.add_argument("--no-endpoints", action="store_true",
                     help="skip the server-endpoint and noise measurements")
@@ -680,7 +682,7 @@ def main():
         result["random32"] = run_random32(args.fw, args.tile, args.engine)
         s32 = CudaPureState(n, "fp32")
     if not args.no_qft and rank == 0:
-        result["qft28_fp64"] = run_qft_fp64()
+        result[f"qft{args.qft_n}_fp64"] = run_qft_fp64(args.qft_n)
     if not args.no_layers and rank == 0:
         result["layers20_shots"] = run_layers_shots()
     if not args.no_endpoints and rank == 0:

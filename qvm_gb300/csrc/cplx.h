@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace qvmg {
 
@@ -49,13 +50,60 @@ __device__ __forceinline__ unsigned long long df_f2d_bits(float f) {
   if (mag == 0) return sign;
   return sign | (((unsigned long long)mag + (896ull << 23)) << 29);
 }
+// Bit moves that compile for the host as well (the integer split below is
+// checked against FP64 arithmetic on the CPU).
+__host__ __device__ __forceinline__ unsigned df_fbits(float f) {
+  unsigned u;
+  memcpy(&u, &f, 4);
+  return u;
+}
+__host__ __device__ __forceinline__ float df_bitsf(unsigned u) {
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+__host__ __device__ __forceinline__ unsigned long long df_dbits(double d) {
+  unsigned long long u;
+  memcpy(&u, &d, 8);
+  return u;
+}
+
+// hi + lo as a double: both convert exactly by bit moves, then one FP64 add
+// (an exact integer form of the rounded sum costs more ALU instructions than
+// the add costs on the 1/64-rate FP64 pipe).
 __device__ __forceinline__ double df_to_double(float hi, float lo) {
   return __longlong_as_double(df_f2d_bits(hi)) + __longlong_as_double(df_f2d_bits(lo));
 }
+
+// x -> (hi, lo) for 2^-74 <= |x| < 2^128 by integer operations and one
+// int -> float conversion: hi is x truncated to 24 bits, lo = RN(x - hi) =
+// RN(r) * 2^(e - 1075) with r the 29 low significand bits (the scale is a
+// normal float in this range, so the product is exact).  Equal bit for bit to
+// the FP64 form below; false outside the range.
+__host__ __device__ __forceinline__ bool df_split_int(double x, float &hi, float &lo) {
+  const unsigned long long u = df_dbits(x);
+  const unsigned long long mag = u & 0x7FFFFFFFFFFFFFFFull;
+  if (mag < (949ull << 52) || mag >= (1151ull << 52)) return false;
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  hi = df_bitsf((unsigned)((mag >> 29) - (896ull << 23)) | sign);
+  const unsigned r = (unsigned)(mag & ((1ull << 29) - 1ull));
+  const unsigned e = (unsigned)(mag >> 52);
+  const float scale = df_bitsf((e - 948u) << 23);  // 2^(e - 1075)
+#ifdef __CUDA_ARCH__
+  const float rf = __uint2float_rn(r);
+#else
+  const float rf = (float)r;  // round to nearest (the host's default mode)
+#endif
+  lo = r ? df_bitsf(df_fbits(rf * scale) | sign) : 0.f;
+  return true;
+}
+
 // x -> (hi, lo): hi is x truncated to 24 bits by integer operations, lo the
-// rounded remainder (one FP64 subtraction, exact, and one conversion).
-// |x| below 2^-126 goes entirely to lo.  |x| must be below 2^128.
+// rounded remainder (one FP64 subtraction, exact, and one conversion) where
+// the integer form does not apply.  |x| below 2^-126 goes entirely to lo.
+// |x| must be below 2^128.
 __device__ __forceinline__ void df_split(double x, float &hi, float &lo) {
+  if (df_split_int(x, hi, lo)) return;
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const unsigned long long mag = u & 0x7FFFFFFFFFFFFFFFull;
   if (mag < (897ull << 52)) {
