@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-32q", action="store_true", help="skip the 32-qubit random circuit")
     ap.add_argument("--no-endpoints", action="store_true",
                     help="skip the server-endpoint and noise measurements")
+    ap.add_argument("--no-plain-passes", action="store_true",
+                    help="skip the per-kind timing of memory-bound plain passes")
     ap.add_argument("--no-layers", action="store_true",
                     help="skip the 20-qubit layer circuit with 1000 shots")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -215,9 +217,9 @@ def run_qft_fp64(n: int = 28, seed: int = 2, runs: int = 3):
     """28-qubit QFT in complex FP64, plain kernels (one pass per H and SWAP,
     one phase-table pass per CPHASE chain) on a random normalised state of
     complex N(0,1) amplitudes.  Reports gates/s and HBM GB/s per pass kind,
-    from CUDA events around every pass.  Algorithmic bytes per pass: dense
-    and phase passes read and write every amplitude (2 * 16 * 2^n); a SWAP
-    moves half of them (2 * 16 * 2^(n-1))."""
+    from CUDA events around every pass.  Algorithmic bytes per pass: a dense
+    pass reads and writes every amplitude (2 * 16 * 2^n); a phase pass and a
+    SWAP the half they change (2 * 16 * 2^(n-1))."""
     from qvm_gb300 import CudaPureState, Program, circuits
     gates = circuits.qft(n)
     rng = np.random.default_rng(seed)
@@ -232,7 +234,10 @@ def run_qft_fp64(n: int = 28, seed: int = 2, runs: int = 3):
     prog.run(s, fused=False)  # untimed: uploads the plan
     s.sync()
     amp = 16 * (1 << n)
-    bytes_of = {0: 2 * amp, 1: 2 * amp, 2: amp}   # dense, diagonal table, permutation
+    # dense: every amplitude read and written; a CPHASE chain's phase pass: the
+    # half with the target bit set (the others keep phase 1 and are not
+    # visited); a SWAP: the half it moves
+    bytes_of = {0: 2 * amp, 1: amp, 2: amp}
     names = {0: "dense", 1: "phase", 2: "swap"}
     best = None
     for _ in range(runs):
@@ -258,6 +263,52 @@ def run_qft_fp64(n: int = 28, seed: int = 2, runs: int = 3):
             "gates_per_s": len(gates) / (total / 1e3),
             "hbm_GB_per_s": moved / (total / 1e3) / 1e9,
             "frac_of_measured_peak": moved / (total / 1e3) / 1e9 / peak, "per_pass_kind": per}
+
+
+def run_plain_passes(runs: int = 5, seed: int = 9):
+    """Memory-bound plain passes, one per kind, on an 8 GiB state: FP32 at 30
+    qubits and FP64 at 29.  Each gate below is one pass, timed with CUDA events
+    around every pass; algorithmic bytes count the amplitudes a pass reads and
+    writes: a dense 1-/2-qubit gate and RZ every amplitude (2*b*N), CPHASE the
+    quarter whose phase is not 1, X every amplitude, CNOT and SWAP the half they
+    move."""
+    from qvm_gb300 import CudaPureState, Program, circuits, gates as G
+    rng = np.random.default_rng(seed)
+    peak, _ = peaks()
+    out = {}
+    for prec, n in (("fp32", 30), ("fp64", 29)):
+        b = 8 if prec == "fp32" else 16
+        N = float(1 << n)
+        # (label, matrix, nat-tuple qubits, bytes)
+        seq = [("H q29" if n == 30 else "H q28", G.gate_matrix("H"), [n - 1], 2 * b * N),
+               ("RZ q5", G.gate_matrix("RZ", 0.3), [5], 2 * b * N),
+               ("H q0", G.gate_matrix("H"), [0], 2 * b * N),
+               ("SU4 q3,q27", circuits.haar_special_unitary(rng, 4), [27, 3], 2 * b * N),
+               ("CPHASE q2,q9", G.gate_matrix("CPHASE", 0.1), [9, 2], 2 * b * N / 4),
+               ("X q7", G.gate_matrix("X"), [7], 2 * b * N),
+               ("CNOT q28,q4" if n == 30 else "CNOT q27,q4", G.gate_matrix("CNOT"),
+                [4, n - 2], b * N),
+               ("SWAP q1,q20", G.gate_matrix("SWAP"), [20, 1], b * N)]
+        prog = Program()
+        prog.add_gates([(m, q) for _, m, q, _ in seq])
+        prog.plan(n, prec, fused=False)
+        s = CudaPureState(n, prec)
+        prog.run(s, fused=False)
+        best = None
+        for _ in range(runs):
+            ms, kinds = prog.run_profiled(s, fused=False)
+            best = ms if best is None else np.minimum(best, ms)
+        s.free()
+        prog.free()
+        if len(best) != len(seq):
+            out[prec] = {"error": f"{len(best)} passes for {len(seq)} gates"}
+            continue
+        rows = {}
+        for (label, _, _, by), t in zip(seq, best):
+            gbs = by / (t / 1e3) / 1e9
+            rows[label] = {"ms": float(t), "GB_per_s": gbs, "frac_of_measured_peak": gbs / peak}
+        out[prec] = {"qubits": n, "passes": rows}
+    return out
 
 
 def run_layers_shots(n: int = 20, layers: int = 10, shots: int = 1000, seed: int = 1, runs: int = 5):
@@ -683,6 +734,8 @@ def main():
         s32 = CudaPureState(n, "fp32")
     if not args.no_qft and rank == 0:
         result[f"qft{args.qft_n}_fp64"] = run_qft_fp64(args.qft_n)
+    if not args.no_plain_passes and rank == 0:
+        result["plain_passes"] = run_plain_passes()
     if not args.no_layers and rank == 0:
         result["layers20_shots"] = run_layers_shots()
     if not args.no_endpoints and rank == 0:

@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(256)
 
 constexpr int kMaxTables = 4;
 constexpr int kMaxTableBits = 10;
+constexpr int kMaxReq = 4;
 
 struct DiagArgs {
   int ntables;
@@ -107,6 +108,12 @@ struct DiagArgs {
   // A CPHASE chain's table -- a run of controls plus its target -- is one.
   int lo1[kMaxTables], n1[kMaxTables], lo2[kMaxTables];
   int total;              // total entries
+  // Required qubits, ascending: every table holds them, and every entry with
+  // one of them 0 is exactly 1 (a CPHASE's or CZ's two qubits, a CPHASE
+  // chain's target).  Only amplitudes with all of them 1 can change, so the
+  // kernels visit 2^(n - nreq) indices with those bits set.
+  int nreq;
+  int req[kMaxReq];
 };
 
 __device__ __forceinline__ int diag_index(const DiagArgs &p, int t, uint64_t i) {
@@ -121,9 +128,30 @@ __device__ __forceinline__ int diag_index(const DiagArgs &p, int t, uint64_t i) 
   return idx;
 }
 
+// Index j of the visited subspace -> amplitude address: a 1 inserted at each
+// required qubit (ascending).
+__device__ __forceinline__ uint64_t diag_address(const DiagArgs &p, uint64_t j) {
+  for (int r = 0; r < p.nreq; ++r) j = inject0(j, p.req[r]) | (1ull << p.req[r]);
+  return j;
+}
+
 // The product of an amplitude's table entries is formed in double-float
 // (dfc, cplx.h: FP32 pairs, ~47-bit significand) on the FP32 pipe; on this
 // part the FP64 pipe runs at 1/64 of the FP32 rate.
+
+// Product of an FP32 amplitude's table entries other than 1 ((1, 0) if none).
+__device__ __forceinline__ float2 diag_phase_f32(const DiagArgs &p, const float2 *tab,
+                                                 uint64_t i) {
+  float2 ph = make_float2(1.f, 0.f);
+  bool unit = true;
+  for (int t = 0; t < p.ntables; ++t) {
+    const float2 e = tab[p.start[t] + diag_index(p, t, i)];
+    if (e.x == 1.f && e.y == 0.f) continue;
+    ph = unit ? e : cmul(ph, e);
+    unit = false;
+  }
+  return ph;
+}
 
 // FP32 states: tables and products in FP32.  Entries equal to 1 are
 // skipped, and an amplitude whose phase is 1 is neither read nor written.
@@ -134,17 +162,29 @@ __global__ void __launch_bounds__(256)
   float2 *tab = reinterpret_cast<float2 *>(smem_raw);
   for (int j = threadIdx.x; j < p.total; j += blockDim.x) tab[j] = tables[j];
   __syncthreads();
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    float2 ph = make_float2(1.f, 0.f);
-    bool unit = true;
-    for (int t = 0; t < p.ntables; ++t) {
-      const float2 e = tab[p.start[t] + diag_index(p, t, i)];
-      if (e.x == 1.f && e.y == 0.f) continue;
-      ph = unit ? e : cmul(ph, e);
-      unit = false;
+  const uint64_t count = len >> p.nreq;
+  if (p.nreq == 0 || p.req[0] > 0) {
+    // Qubit 0 is not required: a thread takes the two amplitudes at i and
+    // i + 1, one 16-byte load and store (a pair without a phase is skipped).
+    float4 *a4 = reinterpret_cast<float4 *>(a);
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count / 2;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+      const uint64_t i = diag_address(p, 2 * j);
+      const float2 ph0 = diag_phase_f32(p, tab, i), ph1 = diag_phase_f32(p, tab, i + 1);
+      const bool u0 = ph0.x == 1.f && ph0.y == 0.f, u1 = ph1.x == 1.f && ph1.y == 0.f;
+      if (u0 && u1) continue;
+      const float4 v = a4[i >> 1];
+      const float2 r0 = u0 ? make_float2(v.x, v.y) : cmul(make_float2(v.x, v.y), ph0);
+      const float2 r1 = u1 ? make_float2(v.z, v.w) : cmul(make_float2(v.z, v.w), ph1);
+      a4[i >> 1] = make_float4(r0.x, r0.y, r1.x, r1.y);
     }
-    if (!unit && (ph.x != 1.f || ph.y != 0.f)) a[i] = cmul(a[i], ph);
+    return;
+  }
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count;
+       j += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = diag_address(p, j);
+    const float2 ph = diag_phase_f32(p, tab, i);
+    if (ph.x != 1.f || ph.y != 0.f) a[i] = cmul(a[i], ph);
   }
 }
 
@@ -164,8 +204,10 @@ __global__ void __launch_bounds__(256)
     tab[j] = d;
   }
   __syncthreads();
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
-       i += (uint64_t)gridDim.x * blockDim.x) {
+  const uint64_t count = len >> p.nreq;
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count;
+       j += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = diag_address(p, j);
     dfc ph;
     int nonunit = 0;
     for (int t = 0; t < p.ntables; ++t) {
@@ -274,6 +316,30 @@ static int perm_dispatch(qvmg_state s, int k, const int *qubits, const int64_t *
   return fail(QVMG_E_INVALID, "permutation width must be 1..5");
 }
 
+int diag_required_bits(int ntables, const int *ks, const int *qubits, const double *tables,
+                       int *req) {
+  int nreq = 0;
+  for (int j0 = 0; j0 < ks[0] && nreq < kMaxReq; ++j0) {
+    const int q = qubits[j0];
+    bool ok = true;
+    int qoff = 0, eoff = 0;
+    for (int t = 0; t < ntables && ok; ++t) {
+      int pos = -1;
+      for (int j = 0; j < ks[t]; ++j)
+        if (qubits[qoff + j] == q) pos = j;
+      if (pos < 0) ok = false;
+      for (int e = 0; ok && e < (1 << ks[t]); ++e)
+        if (!((e >> pos) & 1) && (tables[2 * (eoff + e)] != 1.0 || tables[2 * (eoff + e) + 1] != 0.0))
+          ok = false;
+      qoff += ks[t];
+      eoff += 1 << ks[t];
+    }
+    if (ok) req[nreq++] = q;
+  }
+  std::sort(req, req + nreq);
+  return nreq;
+}
+
 static int diag_args(int ntables, const int *ks, const int *qubits, DiagArgs &p) {
   std::memset(&p, 0, sizeof(p));
   p.ntables = ntables;
@@ -328,6 +394,7 @@ static int diag_tables_impl(qvmg_state s, int ntables, const int *ks, const int 
   using C = typename CT<T>::C;
   DiagArgs p;
   int total = diag_args(ntables, ks, qubits, p);
+  p.nreq = diag_required_bits(ntables, ks, qubits, tables, p.req);
   std::vector<C> host(total);
   for (int i = 0; i < total; ++i) host[i] = CT<T>::make((T)tables[2 * i], (T)tables[2 * i + 1]);
   int rc = ensure_dvec(s, total * sizeof(C));
@@ -369,13 +436,16 @@ int launch_diag_tables(qvmg_state s, int ntables, const int *ks, const int *qubi
 }
 
 int launch_diag_dev(qvmg_state s, int ntables, const int *ks, const int *qubits,
-                    const void *dtables) {
+                    const void *dtables, int nreq, const int *req) {
   if (ntables < 1 || ntables > kMaxTables)
     return fail(QVMG_E_INVALID, "diagonal pass needs 1..4 tables");
+  if (nreq < 0 || nreq > kMaxReq) return fail(QVMG_E_INVALID, "too many required qubits");
   int rc = diag_attr();
   if (rc) return rc;
   DiagArgs p;
   diag_args(ntables, ks, qubits, p);
+  p.nreq = nreq;
+  for (int r = 0; r < nreq; ++r) p.req[r] = req[r];
   if (s->prec == QVMG_FP64) return diag_dev_impl<double>(s, p, dtables);
   return diag_dev_impl<float>(s, p, dtables);
 }

@@ -120,7 +120,12 @@ int launch_diag_tables(qvmg_state s, int ntables, const int *ks, const int *qubi
                        const double *tables);
 // Same, with the tables already in device memory in the state's precision.
 int launch_diag_dev(qvmg_state s, int ntables, const int *ks, const int *qubits,
-                    const void *dtables);
+                    const void *dtables, int nreq, const int *req);
+// Qubits every table holds whose 0 value makes every entry exactly 1 (at
+// most 4, ascending); tables are interleaved (re, im) doubles.  Returns their
+// count.
+int diag_required_bits(int ntables, const int *ks, const int *qubits, const double *tables,
+                       int *req);
 
 
 }  // namespace qvmg

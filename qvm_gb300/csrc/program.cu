@@ -38,6 +38,7 @@ struct DevicePlan {
   std::vector<TileArgs> tile_args;      // per pass (TILE passes)
   std::vector<std::vector<int>> dks;    // per pass (DIAG passes): table widths
   std::vector<std::vector<int>> dqs;    // per pass (DIAG passes): flat qubits
+  std::vector<std::vector<int>> dreq;   // per pass (DIAG passes): required qubits
   bool has_tc = false;                  // some tile pass runs tensor-core ops
   ~DevicePlan() {
     if (buf) cudaFree(buf);
@@ -86,17 +87,27 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
   dp.tile_args.assign(dp.plan.passes.size(), TileArgs{});
   dp.dks.assign(dp.plan.passes.size(), {});
   dp.dqs.assign(dp.plan.passes.size(), {});
+  dp.dreq.assign(dp.plan.passes.size(), {});
   for (size_t i = 0; i < dp.plan.passes.size(); ++i) {
     const Pass &ps = dp.plan.passes[i];
     align16(bytes);
     dp.pass_off[i] = bytes.size();
     if (ps.kind == Pass::DIAG) {
+      std::vector<double> flat;
       for (size_t t = 0; t < ps.tq.size(); ++t) {
         dp.dks[i].push_back((int)ps.tq[t].size());
         for (int q : ps.tq[t]) dp.dqs[i].push_back(q);
         if (prec == QVMG_FP64) put_complex<double>(bytes, ps.tables[t]);
         else put_complex<float>(bytes, ps.tables[t]);
+        for (const cd &z : ps.tables[t]) {
+          flat.push_back(z.real());
+          flat.push_back(z.imag());
+        }
       }
+      int req[4];
+      const int nreq = diag_required_bits((int)dp.dks[i].size(), dp.dks[i].data(),
+                                          dp.dqs[i].data(), flat.data(), req);
+      dp.dreq[i].assign(req, req + nreq);
     } else if (ps.kind == Pass::TILE) {
       TileArgs &ta = dp.tile_args[i];
       std::memset(&ta, 0, sizeof(ta));
@@ -234,7 +245,8 @@ static int run_device_plan(qvmg_state s, DevicePlan &dp, cudaEvent_t *events = n
         break;
       case Pass::DIAG:
         rc = launch_diag_dev(s, (int)dp.dks[i].size(), dp.dks[i].data(), dp.dqs[i].data(),
-                             (const unsigned char *)dp.buf + dp.pass_off[i]);
+                             (const unsigned char *)dp.buf + dp.pass_off[i],
+                             (int)dp.dreq[i].size(), dp.dreq[i].data());
         break;
       case Pass::TILE: {
         TileArgs ta = dp.tile_args[i];
