@@ -711,13 +711,13 @@ __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
 // (0: every stage runs in shared memory).  Narrow instantiations keep the
 // register arrays of wide cases out of the kernel.
 // Threads of a tile CTA: 256, plus the MMA-issuing warp in tensor-core kernels.
-template <int RB>
+template <typename T, int RB>
 constexpr int tile_threads() {
-  return RB < 0 ? kTileThreads + 32 : kTileThreads;
+  return RB == 0 && !kIsDf<T> ? kTileThreadsSmem : (RB < 0 ? kTileThreads + 32 : kTileThreads);
 }
 
 template <typename T, int KMAX, int RB>
-__global__ void __launch_bounds__(tile_threads<RB>(), (RB == 5 || RB < 0) ? 2 : (KMAX <= 2 ? 3 : 1))
+__global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2 : (KMAX <= 2 ? 3 : 1))
     k_tile(typename GT<T>::G *__restrict__ a, const __grid_constant__ TileArgs p) {
   using C = typename CT<T>::C;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -887,7 +887,7 @@ static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
   // shared memory), each looping over tiles.
   int per_sm = 0;
   QVMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<T, KMAX, RB>,
-                                                          tile_threads<RB>(), smem));
+                                                          tile_threads<T, RB>(), smem));
   if (per_sm < 1) return fail(QVMG_E_UNSUPPORTED, "tile pass does not fit on an SM");
   if (RB < 0) {
     // The occupancy query answers 1 for kernels that allocate tensor memory;
@@ -911,11 +911,11 @@ static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
       return e;
     }));
     const int by_smem = smem_sm / (int)(smem + (size_t)stat + 1024);
-    const int by_regs = 65536 / (((regs * 32 + 255) / 256) * 256 * (tile_threads<RB>() / 32));
+    const int by_regs = 65536 / (((regs * 32 + 255) / 256) * 256 * (tile_threads<T, RB>() / 32));
     per_sm = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTcCols));
   }
   uint64_t grid = std::min<uint64_t>(args.ntiles, (uint64_t)sm_count() * per_sm);
-  k_tile<T, KMAX, RB><<<(unsigned)grid, tile_threads<RB>(), smem, s->stream>>>(
+  k_tile<T, KMAX, RB><<<(unsigned)grid, tile_threads<T, RB>(), smem, s->stream>>>(
       (typename GT<T>::G *)s->amps, args);
   QVMG_CHECK_LAUNCH("k_tile");
   return QVMG_OK;

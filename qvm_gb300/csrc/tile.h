@@ -6,7 +6,15 @@
 
 namespace qvmg {
 
-constexpr int kTileThreads = 256;
+constexpr int kTileThreads = 256;  // register-stage and tensor-core kernels
+// FP32 kernels whose ops all run over shared memory (the FMA engine).  Every
+// thread repeats each op's setup (sorted positions, offsets, the hoisted
+// block matrix) for every tile, so fewer threads per tile do less of it: 128
+// threads and 3 CTAs per SM took the 30-qubit depth-20 circuit from 296 to
+// 278 ms (256 and 192 threads, and 64 threads with 6-8 CTAs per SM, were
+// slower at 13-qubit tiles).  FP64 double-float tiles keep 256 threads: 128
+// took the fused 28-qubit circuit from 522 to 537 ms.
+constexpr int kTileThreadsSmem = 128;
 // Dynamic shared memory of a tile pass: the 227 KiB a CTA may hold, less
 // 64 bytes for the kernel's static shared variables (MMA barrier, TMEM slot).
 constexpr int kTileMaxSmem = 227 * 1024 - 64;
