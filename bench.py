@@ -95,7 +95,7 @@ def whole_job_rate(units_per_rank_step: int, steps: int, world: int, max_ms: flo
 # the ncu captures summarised under profiles/ (k_tile_fp32_random26_fw2_t13,
 # k_tile_tc_fp32_random26_fw4_t13).  Traffic per launch grows with the
 # amplitudes processed, so a launch at n qubits moves 2^(n-26) times as much.
-TILE_TRAFFIC_26Q = {"fma": 536.917504e6 + 475.407360e6, "tc": 536.962816e6 + 478.344448e6}
+TILE_TRAFFIC_26Q = {"fma": 536.926208e6 + 475.259648e6, "tc": 536.962816e6 + 478.344448e6}
 
 
 def traffic_per_launch(n, engine):
