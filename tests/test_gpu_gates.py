@@ -110,6 +110,44 @@ def test_permutation_and_diagonal(gpu, oracle, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_diagonal_required_qubits(gpu, oracle, prec):
+    """Diagonal passes visit only the amplitudes whose required qubits (held
+    by every table, with every entry for their 0 value exactly 1) are set.
+    Cases: CZ with qubit 0 (the FP32 single-amplitude path), CPHASE, a
+    3-qubit controlled phase, unit entries that make no qubit required, one
+    required qubit beside one that is not, and a CPHASE chain with a lone CZ
+    through the program's plain plan."""
+    n = 12
+    rng = np.random.default_rng(21)
+    ph = lambda: np.exp(1j * rng.uniform(0.1, 2 * np.pi - 0.1))  # never exactly 1
+    cases = [
+        ([0, 5], np.array([1, 1, 1, -1], dtype=complex)),                  # CZ: {0, 5}
+        ([9, 3], np.array([1, 1, 1, ph()])),                               # CPHASE: {3, 9}
+        ([11, 6, 1], np.array([1] * 7 + [ph()])),                          # {1, 6, 11}
+        ([2, 7], np.array([ph(), 1, 1, ph()])),                            # none
+        ([4, 8], np.array([1, ph(), 1, ph()])),                            # {4}
+        ([10], np.array([1, ph()])),                                       # PHASE: {10}
+    ]
+    wf = circuits.random_state(n, seed=5)
+    s = upload(wf, prec)
+    want = wf.copy()
+    for qs, d in cases:
+        s.apply_diagonal(d, qs)
+        _apply_table(want, qs, d)
+        assert np.max(np.abs(s.state_elements() - want)) < tol(prec), (qs, prec)
+    s.free()
+    # the same through a program: a CPHASE chain on target 9 (one table pass),
+    # then a lone CZ 0 11, each separated by an H so that they stay separate passes
+    gs = [(gates.gate_matrix("H"), [9])]
+    gs += [(gates.gate_matrix("CPHASE", np.pi / 2 ** (9 - j)), [9, j]) for j in range(9)]
+    gs += [(gates.gate_matrix("H"), [3]), (gates.gate_matrix("CZ"), [11, 0]),
+           (gates.gate_matrix("H"), [0])]
+    want = _oracle(oracle, gs, n, init=wf)
+    got = _run_program(gs, n, prec, fused=False, init=wf).state_elements()
+    assert np.max(np.abs(got - want)) < tol(prec) * 4
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_standard_gates(gpu, oracle, prec):
     """Every standard gate through apply_dense (which routes permutation and
     diagonal matrices to their kernels)."""
