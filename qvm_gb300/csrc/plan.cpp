@@ -304,7 +304,10 @@ size_t tile_pass_smem_bytes(const Pass &p, int prec) {
   size_t rows = (((size_t)1 << (p.t - p.L)) + 1) & ~(size_t)1;
   size_t b = ((size_t)1 << p.t) * csz + rows * 8;
   // (+ csz: a tensor-core operand starts on a 16-byte boundary)
-  for (auto &o : p.tops) b += o.data.size() * csz + kTileOpDescBytes + (o.kind == OP_TC ? csz : 0);
+  // (diagonal tables are read from global memory, not staged)
+  for (auto &o : p.tops)
+    b += (o.kind == OP_DIAG ? 0 : o.data.size() * csz) + kTileOpDescBytes +
+         (o.kind == OP_TC ? csz : 0);
   b += p.stages.size() * kTileStageDescBytes;
   return (b + 15) & ~(size_t)15;
 }

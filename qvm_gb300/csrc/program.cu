@@ -77,6 +77,57 @@ static void align16(std::vector<unsigned char> &bytes) {
   while (bytes.size() % 16) bytes.push_back(0);
 }
 
+// A diagonal tile op's index layout inside its pass's tiles (TileDiagInfo):
+// the tile bit of every table qubit, the in-tile bits as runs, and the
+// required qubits (every table entry with one of them 0 is exactly 1).
+static void fill_diag_info(TileOpDev &d, const TileOpHost &th, const Pass &ps) {
+  TileDiagInfo info;
+  std::memset(&info, 0, sizeof(info));
+  const int k = (int)th.pos.size();
+  for (int i = 0; i < k; ++i) {
+    const int q = th.pos[i];
+    int tp = 255;
+    if (q < ps.L) tp = q;
+    for (size_t e = 0; e < ps.E.size(); ++e)
+      if (ps.E[e] == q) tp = ps.L + (int)e;
+    info.tpos[i] = (unsigned char)tp;
+  }
+  // in-tile bits as runs of consecutive index bits on consecutive tile bits
+  int nruns = 0;
+  for (int i = 0; i < k;) {
+    if (info.tpos[i] == 255) {
+      ++i;
+      continue;
+    }
+    int len = 1;
+    while (i + len < k && info.tpos[i + len] != 255 && info.tpos[i + len] == info.tpos[i] + len)
+      ++len;
+    if (nruns < 4) {
+      info.run_t[nruns] = info.tpos[i];
+      info.run_n[nruns] = (unsigned char)len;
+      info.run_i[nruns] = (unsigned char)i;
+    }
+    ++nruns;
+    i += len;
+  }
+  info.nruns = nruns <= 4 ? (unsigned char)nruns : 255;
+  // required qubits
+  std::vector<int> req_t;
+  for (int i = 0; i < k; ++i) {
+    bool req = true;
+    for (size_t e = 0; e < th.data.size() && req; ++e)
+      if (!((e >> i) & 1) && th.data[e] != cd(1.0, 0.0)) req = false;
+    if (!req) continue;
+    if (info.tpos[i] == 255) info.out_req |= (unsigned short)(1u << i);
+    else req_t.push_back(info.tpos[i]);
+  }
+  std::sort(req_t.begin(), req_t.end());
+  if (req_t.size() > 4) req_t.resize(4);  // the rest are visited and skipped as unit
+  info.nreq = (unsigned char)req_t.size();
+  for (size_t r = 0; r < req_t.size(); ++r) info.req_t[r] = (unsigned char)req_t[r];
+  std::memcpy(d.src, &info, sizeof(info));
+}
+
 static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw, int tile,
                              DevicePlan &dp, cudaStream_t stream) {
   make_plan(p->ops, nq, prec, mode, fw, tile, dp.plan, p->reg_stages != 0,
@@ -122,6 +173,7 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
       std::vector<TileOpDev> descs(ps.tops.size());
       int ndata = 0;
       std::vector<cd> data;
+      std::vector<cd> tables;  // diagonal tables: global memory, not shared
       for (size_t o = 0; o < ps.tops.size(); ++o) {
         const TileOpHost &th = ps.tops[o];
         TileOpDev &d = descs[o];
@@ -139,6 +191,12 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
           dp.has_tc = true;
         }
         else if (th.kind != OP_DIAG) ta.kmax = std::max(ta.kmax, d.k);
+        if (th.kind == OP_DIAG) {
+          fill_diag_info(d, th, ps);
+          d.data = (int)tables.size();
+          tables.insert(tables.end(), th.data.begin(), th.data.end());
+          continue;
+        }
         if (th.kind == OP_PERM) {
           int nm = 0;
           for (size_t j = 0; j < th.perm.size(); ++j)
@@ -195,10 +253,29 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
       size_t stages_off = bytes.size();
       bytes.resize(stages_off + sdev.size() * sizeof(TileStageDev));
       std::memcpy(bytes.data() + stages_off, sdev.data(), sdev.size() * sizeof(TileStageDev));
+      align16(bytes);
+      // Diagonal tables stay in global memory (read through the L1 cache):
+      // staged in shared memory, a pass's tables (a CPHASE chain of a QFT
+      // takes up to 3 x 1024 entries) left room for one CTA per SM.  FP64
+      // plans hold them as double-float pairs, rounded on the host exactly as
+      // the device rounds op data (hi = RN(x), lo = RN(x - hi)).
+      size_t tables_off = bytes.size();
+      if (prec == QVMG_FP64) {
+        for (const cd &z : tables) {
+          const float v[4] = {(float)z.real(), (float)(z.real() - (double)(float)z.real()),
+                              (float)z.imag(), (float)(z.imag() - (double)(float)z.imag())};
+          const size_t at = bytes.size();
+          bytes.resize(at + sizeof(v));
+          std::memcpy(bytes.data() + at, v, sizeof(v));
+        }
+      } else {
+        put_complex<float>(bytes, tables);
+      }
       // pointers are patched after upload
       ta.data = (const void *)data_off;
       ta.ops = (const void *)ops_off;
       ta.stages = (const void *)stages_off;
+      ta.tables = (const void *)tables_off;
       if (tile_smem_bytes(prec, ta.t, ta.L, ta.ndata, ta.nops, ta.nstages) > (size_t)kTileMaxSmem)
         return fail(QVMG_E_UNSUPPORTED, "tile pass data exceeds shared memory");
     }
@@ -220,6 +297,7 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
     ta.data = (const unsigned char *)dp.buf + (size_t)ta.data;
     ta.ops = (const unsigned char *)dp.buf + (size_t)ta.ops;
     ta.stages = (const unsigned char *)dp.buf + (size_t)ta.stages;
+    ta.tables = (const unsigned char *)dp.buf + (size_t)ta.tables;
   }
   return QVMG_OK;
 }

@@ -241,19 +241,58 @@ __device__ __forceinline__ void tile_perm(typename CT<T>::C *tile, int t, const 
   }
 }
 
+// Table index of tile element j: the out-of-tile bits (cidx, fixed per
+// tile) plus the in-tile bits read as runs or bit by bit (TileDiagInfo).
+__device__ __forceinline__ int diag_tile_index(const TileDiagInfo &di, const TileOpDev &op,
+                                               int cidx, unsigned j) {
+  int idx = cidx;
+  if (di.nruns != 255) {
+    for (int r = 0; r < di.nruns; ++r)
+      idx |= (int)((j >> di.run_t[r]) & ((1u << di.run_n[r]) - 1u)) << di.run_i[r];
+  } else {
+    for (int i = 0; i < op.k; ++i)
+      if (di.tpos[i] != 255) idx |= (int)((j >> di.tpos[i]) & 1u) << i;
+  }
+  return idx;
+}
+
+// The out-of-tile index bits of this tile (from its base address, the
+// offset of row 0), or -1 if a required qubit outside the tile is 0 here
+// (every entry the tile would use is 1).
+__device__ __forceinline__ int diag_tile_const(const TileDiagInfo &di, const TileOpDev &op,
+                                               const unsigned long long *rowoff) {
+  const unsigned long long base = rowoff[0];
+  int cidx = 0;
+  for (int i = 0; i < op.k; ++i)
+    if (di.tpos[i] == 255) cidx |= (int)((base >> op.pos[i]) & 1ull) << i;
+  return (cidx & di.out_req) == di.out_req ? cidx : -1;
+}
+
+// u-th element with the required in-tile bits set (ascending positions).
+__device__ __forceinline__ unsigned diag_tile_element(const TileDiagInfo &di, unsigned u) {
+  for (int r = 0; r < di.nreq; ++r) {
+    const unsigned q = di.req_t[r];
+    u = ((u >> q) << (q + 1)) | (1u << q) | (u & ((1u << q) - 1u));
+  }
+  return u;
+}
+
+// Diagonal op: each element's table entry multiplies it (entries of 1 are
+// skipped).  The table is read in place from global memory through the
+// read-only cache: staging a pass's tables in shared memory (a QFT chain
+// takes up to 3 x 1024 entries) left room for one CTA per SM.
 template <typename T, bool S>
 __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
                                           const unsigned long long *rowoff, const TileOpDev &op,
                                           const typename CT<T>::C *table) {
   using C = typename CT<T>::C;
-  const unsigned n = 1u << t;
-  const unsigned rowmask = (1u << L) - 1u;
-  const int k = op.k;
-  for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
-    unsigned long long g = rowoff[j >> L] | (j & rowmask);
-    int idx = 0;
-    for (int i = 0; i < k; ++i) idx |= (int)((g >> op.pos[i]) & 1ull) << i;
-    C ph = table[idx];
+  const TileDiagInfo &di = *reinterpret_cast<const TileDiagInfo *>(op.src);
+  const int cidx = diag_tile_const(di, op, rowoff);
+  if (cidx < 0) return;
+  const unsigned count = (1u << t) >> di.nreq;
+  for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+    const unsigned j = diag_tile_element(di, u);
+    const C ph = __ldg(table + diag_tile_index(di, op, cidx, j));
     if (ph.x != (T)1 || ph.y != (T)0) {
       const unsigned p = sw<S>(j);
       tile[p] = cmul(tile[p], ph);
@@ -652,24 +691,26 @@ template <bool S>
 __device__ __forceinline__ void tile_diag_df(dfc *tile, int t, int L,
                                              const unsigned long long *rowoff, const TileOpDev &op,
                                              const dfc *table) {
-  const unsigned n = 1u << t;
-  const unsigned rowmask = (1u << L) - 1u;
-  const int k = op.k;
-  for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
-    const unsigned long long g = rowoff[j >> L] | (j & rowmask);
-    int idx = 0;
-    for (int i = 0; i < k; ++i) idx |= (int)((g >> op.pos[i]) & 1ull) << i;
-    const dfc ph = table[idx];
-    if (ph.rh == 1.f && ph.rl == 0.f && ph.ih == 0.f && ph.il == 0.f) continue;
+  const TileDiagInfo &di = *reinterpret_cast<const TileDiagInfo *>(op.src);
+  const int cidx = diag_tile_const(di, op, rowoff);
+  if (cidx < 0) return;
+  const unsigned count = (1u << t) >> di.nreq;
+  for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+    const unsigned j = diag_tile_element(di, u);
+    const float4 e =
+        __ldg(reinterpret_cast<const float4 *>(table) + diag_tile_index(di, op, cidx, j));
+    if (e.x == 1.f && e.y == 0.f && e.z == 0.f && e.w == 0.f) continue;
     const unsigned p = sw<S>(j);
-    tile[p] = df_cmul(tile[p], ph);
+    tile[p] = df_cmul(tile[p], dfc{e.x, e.y, e.z, e.w});
   }
 }
 
 template <typename T, int KMAX, bool S>
 __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
                                         const unsigned long long *rowoff, const TileOpDev &op,
-                                        const typename CT<T>::C *md) {
+                                        const typename CT<T>::C *md, const void *tables) {
+  // diagonal tables are read from global memory (op.data: entry offset)
+  const typename CT<T>::C *gt = reinterpret_cast<const typename CT<T>::C *>(tables) + op.data;
   if (op.kind == 2) {
     switch (op.k) {
       case 1: tile_perm<T, 1, S>(tile, t, op); break;
@@ -690,7 +731,7 @@ __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
         case 5: if constexpr (KMAX >= 5) tile_dense_df<5, S>(tile, t, op, md); break;
       }
     } else {
-      tile_diag_df<S>(tile, t, L, rowoff, op, md);
+      tile_diag_df<S>(tile, t, L, rowoff, op, gt);
     }
   } else {
     if (op.kind == 0) {
@@ -702,7 +743,7 @@ __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
         case 5: if constexpr (KMAX >= 5) tile_dense<T, 5, S>(tile, t, op, md); break;
       }
     } else {
-      tile_diag<T, S>(tile, t, L, rowoff, op, md);
+      tile_diag<T, S>(tile, t, L, rowoff, op, gt);
     }
   }
 }
@@ -828,7 +869,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
           continue;
         }
       }
-      smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data);
+      smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data, p.tables);
       __syncthreads();
     }
     if constexpr (RB < 0) {

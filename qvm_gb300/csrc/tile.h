@@ -34,6 +34,25 @@ struct TileOpDev {
 };
 static_assert(sizeof(TileOpDev) == 128, "TileOpDev layout");
 
+// Where a diagonal op's table index comes from inside a tile, worked out by
+// the planner; it overlays TileOpDev::src/dst of a diagonal op.  Index bit i
+// is the table's qubit pos[i] (global, ascending): a tile bit (tpos[i]) or a
+// qubit outside the tile, whose value is the same for the whole tile.  The
+// in-tile bits are read as up to four runs, ((j >> run_t) & (2^run_n - 1))
+// << run_i, or bit by bit (nruns = 255).  Required qubits are those whose 0
+// value makes every entry exactly 1: inside the tile only the elements with
+// them set are visited (req_t, ascending); outside it (out_req) a tile where
+// one of them is 0 is left alone.
+struct TileDiagInfo {
+  unsigned char nruns;
+  unsigned char nreq;
+  unsigned short out_req;   // index bits of required qubits outside the tile
+  unsigned char tpos[10];   // tile bit of index bit i, 255 outside the tile
+  unsigned char run_t[4], run_n[4], run_i[4];
+  unsigned char req_t[4];
+};
+static_assert(sizeof(TileDiagInfo) <= 64, "TileDiagInfo overlays src/dst");
+
 // One stage of a tile pass (80 bytes): a register run or one shared-memory op.
 struct TileStageDev {
   int reg;    // 1: register run of ops [first, first+count)
@@ -59,6 +78,9 @@ struct TileArgs {
   const void *ops;     // TileOpDev[nops] in device memory
   const void *data;    // complex op data in device memory (state precision)
   const void *stages;  // TileStageDev[nstages] in device memory
+  // diagonal tables in device memory, read in place: float2 entries (FP32)
+  // or double-float pairs (FP64); a diagonal op's data is its entry offset
+  const void *tables;
 };
 
 size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages);
