@@ -81,6 +81,12 @@ const char *qvmg_last_error(void);
 int qvmg_abi_version(void);
 /* Device facts for admission control: SM count, free/total HBM bytes. */
 int qvmg_device_info(int *sm_count, uint64_t *free_bytes, uint64_t *total_bytes);
+/* Grow the device memory pool that states, scratch and plans come from by
+ * `bytes` (in blocks of up to 16 GiB) and keep it: later allocations need no
+ * new mapping, which can stall other threads' CUDA calls while the GPU is
+ * busy.  A server calls it once with its HBM budget; QVMG_E_NOMEM if the
+ * device cannot hold it (what was reserved stays in the pool). */
+int qvmg_device_reserve(uint64_t bytes);
 /* HBM bytes a state of this size and precision holds (16*2^n or 8*2^n plus
  * its reduction scratch); 0 for invalid arguments. */
 uint64_t qvmg_state_bytes(int nqubits, int precision);
@@ -237,6 +243,12 @@ int qvmg_fidelity(qvmg_state a, qvmg_state b, double *fidelity, double *max_abs_
 int qvmg_program_create(qvmg_program *out);
 int qvmg_program_free(qvmg_program p);
 int qvmg_program_add_dense(qvmg_program p, int k, const int *qubits, const double *matrix);
+/* n dense gates in one call: gate i has ks[i] qubits (nat-tuple order, packed
+ * one after another in `qubits`) and a row-major 2^k x 2^k complex matrix
+ * (packed in `matrices`).  Same validation as qvmg_program_add_dense; on an
+ * invalid gate nothing is added. */
+int qvmg_program_add_dense_many(qvmg_program p, int n, const int *ks, const int *qubits,
+                                const double *matrices);
 int qvmg_program_add_permutation(qvmg_program p, int k, const int *qubits, const int64_t *perm);
 int qvmg_program_add_diagonal(qvmg_program p, int k, const int *qubits, const double *diag);
 int qvmg_program_num_ops(qvmg_program p, int *nops);
@@ -274,6 +286,19 @@ int qvmg_program_run_profiled(qvmg_state s, qvmg_program p, int mode, float *pas
 /* The cudaStream_t (as void*) the state's work is ordered on, so a caller
  * can order or time its own work against it. */
 int qvmg_state_stream(qvmg_state s, void **stream);
+
+/* Scheduling class of a state's work when several states share the GPU (the
+ * serving engine; no reference counterpart, whose server runs one QVM per
+ * connection thread, app/src/entry-point.lisp:655-673).
+ *   1: the state's stream gets the device's highest stream priority, so the
+ *      block scheduler starts its kernels' CTAs before those of other streams;
+ *   0: default priority and grids (each tile pass one persistent CTA set);
+ *  -1: default priority, and tile passes run as many short CTAs (16 tiles
+ *      each) rather than persistent ones, so that high-priority work finds
+ *      free SMs within a fraction of a millisecond.
+ * Results do not depend on the class.  The state's queued work is finished
+ * before its stream is replaced. */
+int qvmg_state_set_priority(qvmg_state s, int priority);
 
 /* ---- batched QAOA MaxCut instances -------------------------------------- */
 /* Many uneven QAOA circuits (examples/qaoa.lisp:7-206: H on all qubits, then

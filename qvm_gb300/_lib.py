@@ -38,6 +38,8 @@ SIGNATURES = {
     "qvmg_state_create": (_i, [_i, _i, _vpp]),
     "qvmg_state_free": (_i, [_vp]),
     "qvmg_state_info": (_i, [_vp, _ip, _ip]),
+    "qvmg_state_set_priority": (_i, [_vp, _i]),
+    "qvmg_device_reserve": (_i, [_u64]),
     "qvmg_state_reset": (_i, [_vp]),
     "qvmg_state_upload": (_i, [_vp, _dp]),
     "qvmg_state_download": (_i, [_vp, _dp]),
@@ -68,6 +70,7 @@ SIGNATURES = {
     "qvmg_program_create": (_i, [_vpp]),
     "qvmg_program_free": (_i, [_vp]),
     "qvmg_program_add_dense": (_i, [_vp, _i, _ip, _dp]),
+    "qvmg_program_add_dense_many": (_i, [_vp, _i, _ip, _ip, _dp]),
     "qvmg_program_add_permutation": (_i, [_vp, _i, _ip, _i64p]),
     "qvmg_program_add_diagonal": (_i, [_vp, _i, _ip, _dp]),
     "qvmg_program_num_ops": (_i, [_vp, _ip]),

@@ -58,6 +58,7 @@ struct qvmg_state_s {
   void *amps = nullptr;            // double2* or float2*
   cudaStream_t stream = nullptr;
   int device = 0;
+  int priority = 0;                // qvmg_state_set_priority: -1 yield, 0 default, 1 high
   double *partials = nullptr;      // kReduceBlocks * 2 doubles
   double *block_sums = nullptr;    // 2^(n-kSampleBlockBits) (+1) doubles
   uint64_t nblocks = 0;
@@ -81,6 +82,15 @@ int grid_for(uint64_t work, int threads, int per_sm = 8);
 int sm_count();
 
 // Ensure state scratch buffers are large enough.
+// Device memory of states, their scratch and uploaded plans comes from the
+// stream-ordered allocator (cudaMallocAsync / cudaFreeAsync on the stream
+// that uses it): a plain cudaFree waits for the whole device, which in the
+// serving engine stalled every worker until all queued passes had drained.
+// The device's default pool keeps freed memory for reuse.
+int dev_alloc(void **p, size_t bytes, cudaStream_t s);
+void dev_free(void *p, cudaStream_t s);
+// A library stream for frees that must wait on other streams' events.
+cudaStream_t free_stream();
 int ensure_dvec(qvmg_state s, uint64_t bytes);
 int ensure_staging(qvmg_state s, uint64_t bytes);
 int ensure_pinned(qvmg_state s, uint64_t bytes);

@@ -40,8 +40,26 @@ struct DevicePlan {
   std::vector<std::vector<int>> dqs;    // per pass (DIAG passes): flat qubits
   std::vector<std::vector<int>> dreq;   // per pass (DIAG passes): required qubits
   bool has_tc = false;                  // some tile pass runs tensor-core ops
+  // Streams that ran this plan, each with an event recorded after its last
+  // run: the buffer is freed in the library's free stream after all of them,
+  // without waiting on the host.
+  std::mutex use_mu;
+  std::map<cudaStream_t, cudaEvent_t> uses;
+  void note_use(cudaStream_t s) {
+    std::lock_guard<std::mutex> g(use_mu);
+    cudaEvent_t &ev = uses[s];
+    if (!ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (ev) cudaEventRecord(ev, s);
+  }
   ~DevicePlan() {
-    if (buf) cudaFree(buf);
+    cudaStream_t fs = free_stream();
+    for (auto &u : uses) {
+      if (u.second) {
+        cudaStreamWaitEvent(fs, u.second, 0);
+        cudaEventDestroy(u.second);
+      }
+    }
+    if (buf) dev_free(buf, fs);
   }
 };
 
@@ -282,7 +300,8 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
   }
   (void)csz;
   if (!bytes.empty()) {
-    QVMG_CUDA(cudaMalloc(&dp.buf, bytes.size()));
+    int rc = dev_alloc(&dp.buf, bytes.size(), stream);
+    if (rc) return rc;
     // Upload on the state's stream and wait for it: a plain cudaMemcpy from
     // pageable memory may return before its DMA lands, and it is ordered on
     // the legacy default stream, which the state's non-blocking stream does
@@ -335,6 +354,7 @@ static int run_device_plan(qvmg_state s, DevicePlan &dp, cudaEvent_t *events = n
       }
     }
   }
+  dp.note_use(s->stream);  // the plan's buffer is freed after this stream's passes
   if (dp.has_tc && rc == QVMG_OK) {
     // a tensor-core pass whose bounded MMA wait gave up has set the status word
     int *dstatus = reinterpret_cast<int *>(reinterpret_cast<char *>(s->dres) +
@@ -504,6 +524,34 @@ int qvmg_program_add_dense(qvmg_program p, int k, const int *qubits, const doubl
   for (int i = 0; i < d * d; ++i) op.m[i] = cd(matrix[2 * i], matrix[2 * i + 1]);
   std::lock_guard<std::mutex> g(p->mu);
   p->ops.push_back(std::move(op));
+  p->plans.clear();
+  return QVMG_OK;
+}
+
+int qvmg_program_add_dense_many(qvmg_program p, int n, const int *ks, const int *qubits,
+                                const double *matrices) {
+  if (!p) return fail(QVMG_E_INVALID, "null program");
+  if (n < 0 || (n > 0 && (!ks || !qubits || !matrices)))
+    return fail(QVMG_E_INVALID, "null gate arrays");
+  std::vector<Op> ops;
+  ops.reserve((size_t)n);
+  size_t qoff = 0, moff = 0;
+  for (int i = 0; i < n; ++i) {
+    const int k = ks[i];
+    int rc = check_op_qubits(k, qubits + qoff, QVMG_MAX_GATE_QUBITS);
+    if (rc) return rc;
+    Op op;
+    op.kind = OP_DENSE;
+    op.q.assign(qubits + qoff, qubits + qoff + k);
+    const size_t d = (size_t)1 << k;
+    op.m.resize(d * d);
+    for (size_t j = 0; j < d * d; ++j) op.m[j] = cd(matrices[2 * (moff + j)], matrices[2 * (moff + j) + 1]);
+    qoff += (size_t)k;
+    moff += d * d;
+    ops.push_back(std::move(op));
+  }
+  std::lock_guard<std::mutex> g(p->mu);
+  for (auto &op : ops) p->ops.push_back(std::move(op));
   p->plans.clear();
   return QVMG_OK;
 }

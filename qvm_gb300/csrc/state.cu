@@ -6,6 +6,10 @@
 // copy-wavefunction of the reference (src/state-representation.lisp:76-152,
 // src/allocator.lisp:47-106, src/wavefunction.lisp:80-109).
 #include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <vector>
 #include <stdio.h>
 
 #include <algorithm>
@@ -77,43 +81,111 @@ int check_qubits(qvmg_state s, int k, const int *qubits, int kmax) {
   return QVMG_OK;
 }
 
+int dev_alloc(void **p, size_t bytes, cudaStream_t s) {
+  static std::once_flag flag;
+  static cudaError_t err = cudaSuccess;
+  QVMG_CUDA(once(flag, err, [] {
+    // keep freed memory in the pool: states and plans come and go per request
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    cudaMemPool_t pool;
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    uint64_t keep = ~0ull;
+    if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    return e;
+  }));
+  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_fail(e, "cudaMallocAsync");
+  }
+  return QVMG_OK;
+}
+
+void dev_free(void *p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+cudaStream_t free_stream() {
+  static std::once_flag flag;
+  static cudaStream_t st = nullptr;
+  std::call_once(flag, [] { cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking); });
+  return st;
+}
+
+// Scratch buffers are replaced in the state's stream order: the old one is
+// freed after the work already queued that reads it.
 int ensure_dvec(qvmg_state s, uint64_t bytes) {
   if (s->dvec_bytes >= bytes) return QVMG_OK;
-  if (s->dvec) {
-    QVMG_CUDA(cudaStreamSynchronize(s->stream));
-    cudaFree(s->dvec);
-    s->dvec = nullptr;
-    s->dvec_bytes = 0;
-  }
+  dev_free(s->dvec, s->stream);
+  s->dvec = nullptr;
+  s->dvec_bytes = 0;
   uint64_t want = std::max<uint64_t>(bytes, 1 << 16);
-  QVMG_CUDA(cudaMalloc(&s->dvec, want));
+  int rc = dev_alloc((void **)&s->dvec, want, s->stream);
+  if (rc) return rc;
   s->dvec_bytes = want;
   return QVMG_OK;
 }
 
 int ensure_staging(qvmg_state s, uint64_t bytes) {
   if (s->staging_bytes >= bytes) return QVMG_OK;
-  if (s->staging) {
-    QVMG_CUDA(cudaStreamSynchronize(s->stream));
-    cudaFree(s->staging);
-    s->staging = nullptr;
-    s->staging_bytes = 0;
-  }
-  QVMG_CUDA(cudaMalloc(&s->staging, bytes));
+  dev_free(s->staging, s->stream);
+  s->staging = nullptr;
+  s->staging_bytes = 0;
+  int rc = dev_alloc(&s->staging, bytes, s->stream);
+  if (rc) return rc;
   s->staging_bytes = bytes;
   return QVMG_OK;
+}
+
+// Pinned host blocks by power-of-two size class, kept for reuse for the
+// life of the process: cudaMallocHost / cudaFreeHost per state stalled the
+// serving engine's workers for up to seconds while the GPU was busy.
+static std::mutex g_pinned_mu;
+static std::map<uint64_t, std::vector<void *>> g_pinned_free;
+
+static uint64_t pinned_class(uint64_t bytes) {
+  uint64_t c = 64;
+  while (c < bytes) c <<= 1;
+  return c;
+}
+
+int pinned_get(void **p, uint64_t bytes) {
+  const uint64_t c = pinned_class(bytes);
+  {
+    std::lock_guard<std::mutex> g(g_pinned_mu);
+    auto &v = g_pinned_free[c];
+    if (!v.empty()) {
+      *p = v.back();
+      v.pop_back();
+      return QVMG_OK;
+    }
+  }
+  cudaError_t e = cudaMallocHost(p, c);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_fail(e, "cudaMallocHost");
+  }
+  return QVMG_OK;
+}
+
+void pinned_put(void *p, uint64_t bytes) {
+  if (!p) return;
+  std::lock_guard<std::mutex> g(g_pinned_mu);
+  g_pinned_free[pinned_class(bytes)].push_back(p);
 }
 
 int ensure_pinned(qvmg_state s, uint64_t bytes) {
   if (s->pinned_bytes >= bytes) return QVMG_OK;
   if (s->pinned) {
-    QVMG_CUDA(cudaStreamSynchronize(s->stream));
-    cudaFreeHost(s->pinned);
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));  // copies into it are done
+    pinned_put(s->pinned, s->pinned_bytes);
     s->pinned = nullptr;
     s->pinned_bytes = 0;
   }
-  QVMG_CUDA(cudaMallocHost(&s->pinned, bytes));
-  s->pinned_bytes = bytes;
+  int rc = pinned_get(&s->pinned, bytes);
+  if (rc) return rc;
+  s->pinned_bytes = pinned_class(bytes);
   return QVMG_OK;
 }
 
@@ -270,26 +342,18 @@ int qvmg_state_create(int nqubits, int precision, qvmg_state *out) {
       rc = cuda_fail(e, "cudaStreamCreate");
       break;
     }
-    if ((e = cudaMalloc(&s->amps, s->len * amp_bytes(precision))) != cudaSuccess) {
-      rc = cuda_fail(e, "cudaMalloc(amplitudes)");
+    if ((rc = dev_alloc(&s->amps, s->len * amp_bytes(precision), s->stream))) break;
+    if ((rc = dev_alloc((void **)&s->partials, 2 * kReduceBlocks * sizeof(double), s->stream)))
+      break;
+    if ((rc = dev_alloc((void **)&s->block_sums, (s->nblocks + 1) * sizeof(double), s->stream)))
+      break;
+    if ((rc = dev_alloc((void **)&s->dres, sizeof(MeasResult), s->stream))) break;
+    // pooled memory is not zeroed: the status word must start at 0
+    if ((e = cudaMemsetAsync(s->dres, 0, sizeof(MeasResult), s->stream)) != cudaSuccess) {
+      rc = cuda_fail(e, "cudaMemsetAsync(result)");
       break;
     }
-    if ((e = cudaMalloc(&s->partials, 2 * kReduceBlocks * sizeof(double))) != cudaSuccess) {
-      rc = cuda_fail(e, "cudaMalloc(partials)");
-      break;
-    }
-    if ((e = cudaMalloc(&s->block_sums, (s->nblocks + 1) * sizeof(double))) != cudaSuccess) {
-      rc = cuda_fail(e, "cudaMalloc(block sums)");
-      break;
-    }
-    if ((e = cudaMalloc(&s->dres, sizeof(MeasResult))) != cudaSuccess) {
-      rc = cuda_fail(e, "cudaMalloc(result)");
-      break;
-    }
-    if ((e = cudaMallocHost(&s->hres, sizeof(MeasResult))) != cudaSuccess) {
-      rc = cuda_fail(e, "cudaMallocHost(result)");
-      break;
-    }
+    if ((rc = pinned_get((void **)&s->hres, sizeof(MeasResult)))) break;
   } while (0);
   if (rc == QVMG_OK) rc = qvmg_state_reset(s);
   if (rc != QVMG_OK) {
@@ -304,20 +368,68 @@ int qvmg_state_create(int nqubits, int precision, qvmg_state *out) {
 
 int qvmg_state_free(qvmg_state s) {
   if (!s) return QVMG_OK;
-  if (s->stream) cudaStreamSynchronize(s->stream);
-  if (s->amps) cudaFree(s->amps);
-  if (s->partials) cudaFree(s->partials);
-  if (s->block_sums) cudaFree(s->block_sums);
-  if (s->dres) cudaFree(s->dres);
-  if (s->hres) cudaFreeHost(s->hres);
-  if (s->staging) cudaFree(s->staging);
-  if (s->pinned) cudaFreeHost(s->pinned);
+  // device memory goes back to the pool in this stream's order (work of other
+  // states that read it is ordered into this stream by the cross-state calls);
+  // the pinned host buffers wait for this stream only
+  if (s->stream) {
+    dev_free(s->amps, s->stream);
+    dev_free(s->partials, s->stream);
+    dev_free(s->block_sums, s->stream);
+    dev_free(s->dres, s->stream);
+    dev_free(s->staging, s->stream);
+    dev_free(s->dvec, s->stream);
+    cudaStreamSynchronize(s->stream);
+  }
+  pinned_put(s->hres, sizeof(MeasResult));
+  pinned_put(s->pinned, s->pinned_bytes);
   for (auto &e : s->xfer_ev)
     if (e) cudaEventDestroy(e);
-  if (s->dvec) cudaFree(s->dvec);
   if (s->stream) cudaStreamDestroy(s->stream);
   s->amps = nullptr;
   delete s;
+  return QVMG_OK;
+}
+
+int qvmg_device_reserve(uint64_t bytes) {
+  // in blocks of up to 16 GiB (a 30-qubit FP64 state), allocated together and
+  // then freed into the pool, which keeps them
+  const uint64_t block = 16ull << 30;
+  cudaStream_t st = free_stream();
+  std::vector<void *> got;
+  int rc = QVMG_OK;
+  for (uint64_t done = 0; done < bytes && rc == QVMG_OK;) {
+    const uint64_t b = std::min(block, bytes - done);
+    void *p = nullptr;
+    rc = dev_alloc(&p, b, st);
+    if (rc == QVMG_OK) {
+      got.push_back(p);
+      done += b;
+    }
+  }
+  for (void *p : got) dev_free(p, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  return QVMG_OK;
+}
+
+int qvmg_state_set_priority(qvmg_state s, int priority) {
+  int rc = check_state(s);
+  if (rc) return rc;
+  if (priority < -1 || priority > 1) return fail(QVMG_E_INVALID, "priority must be -1, 0 or 1");
+  int least = 0, greatest = 0;
+  QVMG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  const int want = priority == 1 ? greatest : least;
+  const int have = s->priority == 1 ? greatest : least;
+  if (want != have) {
+    // buffers were allocated in the old stream's order: finish it first
+    QVMG_CUDA(cudaStreamSynchronize(s->stream));
+    cudaStream_t ns = nullptr;
+    QVMG_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, want));
+    cudaStreamDestroy(s->stream);
+    s->stream = ns;
+  }
+  s->priority = priority;
   return QVMG_OK;
 }
 

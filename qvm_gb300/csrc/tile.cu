@@ -956,6 +956,9 @@ static int tile_launch_k(qvmg_state s, const TileArgs &args, size_t smem) {
     per_sm = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTcCols));
   }
   uint64_t grid = std::min<uint64_t>(args.ntiles, (uint64_t)sm_count() * per_sm);
+  // a yielding state (priority -1): short CTAs of 16 tiles each, so that the
+  // block scheduler can start other streams' CTAs between them
+  if (s->priority < 0) grid = std::max<uint64_t>(grid, args.ntiles / 16);
   k_tile<T, KMAX, RB><<<(unsigned)grid, tile_threads<T, RB>(), smem, s->stream>>>(
       (typename GT<T>::G *)s->amps, args);
   QVMG_CHECK_LAUNCH("k_tile");

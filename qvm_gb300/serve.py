@@ -11,7 +11,11 @@ others run is admitted as soon as a worker and enough memory are free.
 Among the queued requests the cheapest one that fits goes first (estimated
 cost = gates x 2^n, FP64 weighted by its slower arithmetic, divided by an
 aging factor that grows with the wait), so small requests are not stuck
-behind a 30-qubit FP64 job and large ones still progress.  Freed states are
+behind a 30-qubit FP64 job and large ones still progress.  A second lane of
+workers takes only cheap requests, so that a small request does not wait for
+a worker while every general worker holds a multi-second job; on the GPU
+cheap requests run on high-priority streams while the others' tile passes
+run as short CTAs, so the block scheduler interleaves them.  Freed states are
 kept in a pool keyed by (qubits, precision) and
 reused, evicted least-recently-used when admission needs their bytes.
 
@@ -73,8 +77,10 @@ class StatePool:
         self.idle.setdefault(key, []).append(s)
         self.idle.move_to_end(key)
 
-    def evict_one(self) -> int:
-        """Free the least recently used idle state; returns its bytes (0 if none)."""
+    def evict_one(self, defer=None) -> int:
+        """Remove the least recently used idle state and free it, or append it
+        to `defer` for the caller to free outside its lock; returns its bytes
+        (0 if none)."""
         if not self.idle:
             return 0
         key = next(iter(self.idle))
@@ -83,7 +89,10 @@ class StatePool:
         if not lst:
             del self.idle[key]
         b = state_bytes(key[0], key[1])
-        s.free()
+        if defer is None:
+            s.free()
+        else:
+            defer.append(s)
         return b
 
     def bytes(self) -> int:
@@ -91,15 +100,29 @@ class StatePool:
 
 
 class Server:
-    def __init__(self, hbm_budget: float = 180e9, workers: int = 16, aging_s: float = 2.0):
+    def __init__(self, hbm_budget: float = 180e9, workers: int = 16, aging_s: float = 2.0,
+                 fast_workers: int = 8, fast_cost: float = 1000.0 * (1 << 24)):
+        """`workers` take any request; `fast_workers` more take only requests
+        whose estimated cost (gates x 2^n, FP64 x 8) is at most `fast_cost`
+        (by default a 1000-gate 24-qubit FP32 program), so that a small
+        request never waits for a worker held by a multi-second job."""
         self.budget = int(hbm_budget)
         self.aging_s = float(aging_s)
+        self.fast_cost = float(fast_cost)
+        if workers + fast_workers > 0:
+            # map the budget's device memory once: growing the pool while
+            # requests run stalls the workers' CUDA calls
+            from . import _lib as L
+            L.lib().qvmg_device_reserve(int(self.budget))  # best effort
         self.reserved = 0              # bytes of running requests + idle pooled states
         self.pool = StatePool()
         self.queue = collections.deque()
         self.cv = threading.Condition()
         self.stop = False
-        self.threads = [threading.Thread(target=self._worker, daemon=True) for _ in range(workers)]
+        self.threads = [threading.Thread(target=self._worker, args=(False,), daemon=True)
+                        for _ in range(workers)]
+        self.threads += [threading.Thread(target=self._worker, args=(True,), daemon=True)
+                         for _ in range(fast_workers)]
         for t in self.threads:
             t.start()
 
@@ -111,7 +134,8 @@ class Server:
         fut = Future()
         with self.cv:
             self.queue.append((req, fut, need))
-            self.cv.notify()
+            # every waiting worker: one of the fast lane may not take this request
+            self.cv.notify_all()
         return fut
 
     @staticmethod
@@ -128,17 +152,21 @@ class Server:
                  for r, _, _ in self.queue]
         return sorted(range(len(self.queue)), key=score.__getitem__)
 
-    def _admit(self):
+    def _admit(self, fast_only: bool = False, evicted=None):
         """The cheapest (aged) queued request that fits, evicting idle pooled
-        states if that makes it fit.  Called with the lock held."""
+        states if that makes it fit (into `evicted`, freed by the caller after
+        it drops the lock); a fast worker takes only cheap requests.  Called
+        with the lock held."""
         for i in self._order():
             req, fut, need = self.queue[i]
+            if fast_only and self.cost(req) > self.fast_cost:
+                continue
             key_state = self.pool.take(req.n, req.precision)
             if key_state is not None:
                 del self.queue[i]
                 return req, fut, need, key_state   # its bytes are already reserved
             while self.reserved + need > self.budget:
-                freed = self.pool.evict_one()
+                freed = self.pool.evict_one(evicted)
                 if freed == 0:
                     break
                 self.reserved -= freed
@@ -148,17 +176,25 @@ class Server:
                 return req, fut, need, None
         return None
 
-    def _worker(self):
+    def _worker(self, fast_only: bool = False):
         while True:
+            evicted = []
             with self.cv:
                 item = None
                 while not self.stop:
-                    item = self._admit()
-                    if item is not None:
+                    item = self._admit(fast_only, evicted)
+                    if item is not None or evicted:
                         break
                     self.cv.wait()
-                if item is None:
-                    return
+            # Evicted states are freed outside the lock.  Their bytes were
+            # released from the budget already: this request's state is
+            # created below, after these frees.
+            for s in evicted:
+                s.free()
+            if item is None:
+                if evicted and not self.stop:
+                    continue
+                return
             req, fut, need, st = item
             t0 = time.perf_counter()
             try:
@@ -166,6 +202,9 @@ class Server:
                     st = CudaPureState(req.n, req.precision)
                 else:
                     st.set_to_zero_state()
+                # cheap requests on a high-priority stream; the others yield
+                # (their tile passes run as short CTAs)
+                st.set_priority(1 if self.cost(req) <= self.fast_cost else -1)
                 prog = Program()
                 prog.add_gates(req.gates)
                 if req.fused:

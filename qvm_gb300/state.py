@@ -97,6 +97,12 @@ class CudaPureState:
     def copy_from(self, other: "CudaPureState"):
         L.call("qvmg_state_copy", self.handle, other.handle)
 
+    def set_priority(self, priority: int):
+        """Scheduling class on a shared GPU: 1 high-priority stream, 0
+        default, -1 yield (tile passes in short CTAs).  Results do not
+        depend on it."""
+        L.call("qvmg_state_set_priority", self.handle, int(priority))
+
     def sync(self):
         L.call("qvmg_state_sync", self.handle)
 
@@ -276,9 +282,17 @@ class Program:
         L.call("qvmg_program_add_diagonal", self._h, len(qubits), _qubit_array(qubits), _dptr(d))
 
     def add_gates(self, gates):
-        """Add (matrix, nat-tuple qubits) pairs as dense ops."""
-        for m, qs in gates:
-            self.add_dense(m, qs)
+        """Add (matrix, nat-tuple qubits) pairs as dense ops, in one call."""
+        gates = list(gates)
+        if not gates:
+            return self
+        ks = np.fromiter((len(qs) for _, qs in gates), dtype=np.int32, count=len(gates))
+        qubits = np.fromiter((int(q) for _, qs in gates for q in qs), dtype=np.int32,
+                             count=int(ks.sum()))
+        mats = np.concatenate([np.asarray(m, dtype=np.complex128).ravel() for m, _ in gates])
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.call("qvmg_program_add_dense_many", self._h, len(gates), ks.ctypes.data_as(ip),
+               qubits.ctypes.data_as(ip), _dptr(mats))
         return self
 
     def set_register_stages(self, enable: bool):

@@ -33,7 +33,7 @@ def _requests():
 def test_same_result_alone_and_in_mix(gpu):
     reqs = _requests()
     alone = {}
-    srv = Server(hbm_budget=8e9, workers=1)
+    srv = Server(hbm_budget=8e9, workers=1, fast_workers=0)
     for r in reqs:
         alone[r.tag] = srv.submit(r).result().shots
     srv.close()
@@ -52,3 +52,31 @@ def test_oversized_request_rejected(gpu):
     with pytest.raises(ValueError):
         srv.submit(Request(20, circuits.qft(20), 1, "fp64"))
     srv.close()
+
+
+def test_priority_classes_give_identical_results(gpu):
+    """qvmg_state_set_priority changes the stream priority and, for -1, the
+    tile-pass grid (short CTAs); the amplitudes are bit-identical."""
+    n = 20
+    gs = circuits.random_su_circuit(n, depth=6, seed=4)
+    from qvm_gb300 import CudaPureState, Program
+    p = Program()
+    p.add_gates(gs)
+    p.plan(n, "fp32", fused=True, fusion_width=2, tile_qubits=12)
+    out = {}
+    for prio in (0, -1, 1, 0):
+        s = CudaPureState(n, "fp32")
+        s.set_priority(prio)
+        p.run(s, fused=True)
+        out.setdefault(prio, []).append(s.state_elements())
+        s.free()
+    ref = out[0][0]
+    for prio, states in out.items():
+        for st in states:
+            np.testing.assert_array_equal(st, ref)
+    with pytest.raises(Exception):
+        s = CudaPureState(4, "fp32")
+        try:
+            s.set_priority(2)
+        finally:
+            s.free()
