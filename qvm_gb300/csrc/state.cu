@@ -95,8 +95,20 @@ int dev_alloc(void **p, size_t bytes, cudaStream_t s) {
     return e;
   }));
   cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e == cudaErrorMemoryAllocation) {
+    // The pool keeps freed blocks; if none is large enough and the device is
+    // full, give the unused ones back (after the frees queued so far) and
+    // retry once.
+    cudaGetLastError();
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess &&
+        cudaDeviceSynchronize() == cudaSuccess && cudaMemPoolTrimTo(pool, 0) == cudaSuccess)
+      e = cudaMallocAsync(p, bytes, s);
+  }
   if (e != cudaSuccess) {
     *p = nullptr;
+    cudaGetLastError();
     return cuda_fail(e, "cudaMallocAsync");
   }
   return QVMG_OK;
