@@ -445,7 +445,24 @@ static std::string describe_plan(const Plan &pl) {
         cplx(ps.tables[t]);
         s += "}";
       }
-      s += "]}";
+      // the qubits the kernel requires set (it visits only those amplitudes)
+      {
+        std::vector<int> ks, qs;
+        std::vector<double> flat;
+        for (size_t t = 0; t < ps.tq.size(); ++t) {
+          ks.push_back((int)ps.tq[t].size());
+          qs.insert(qs.end(), ps.tq[t].begin(), ps.tq[t].end());
+          for (const cd &z : ps.tables[t]) {
+            flat.push_back(z.real());
+            flat.push_back(z.imag());
+          }
+        }
+        int req[4];
+        const int nreq = diag_required_bits((int)ks.size(), ks.data(), qs.data(), flat.data(), req);
+        s += "],\"req\":";
+        ints(std::vector<int>(req, req + nreq));
+        s += "}";
+      }
     } else {
       s += "{\"kind\":\"tile\",\"t\":" + std::to_string(ps.t) + ",\"L\":" + std::to_string(ps.L) +
            ",\"E\":";
@@ -477,6 +494,28 @@ static std::string describe_plan(const Plan &pl) {
         } else {
           s += ",\"data\":";
           cplx(th.data);
+        }
+        if (th.kind == OP_DIAG) {
+          // the index layout the kernel uses inside this pass's tiles
+          TileOpDev d;
+          std::memset(&d, 0, sizeof(d));
+          fill_diag_info(d, th, ps);
+          TileDiagInfo di;
+          std::memcpy(&di, d.src, sizeof(di));
+          std::vector<int> tpos(di.tpos, di.tpos + th.pos.size()), runs, req(di.req_t, di.req_t + di.nreq);
+          if (di.nruns != 255)
+            for (int r = 0; r < di.nruns; ++r) {
+              runs.push_back(di.run_t[r]);
+              runs.push_back(di.run_n[r]);
+              runs.push_back(di.run_i[r]);
+            }
+          s += ",\"tpos\":";
+          ints(tpos);
+          s += ",\"nruns\":" + std::to_string(di.nruns) + ",\"runs\":";
+          ints(runs);
+          s += ",\"req_tile\":";
+          ints(req);
+          s += ",\"out_req\":" + std::to_string(di.out_req);
         }
         s += "}";
       }

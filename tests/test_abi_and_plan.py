@@ -229,3 +229,96 @@ def test_plan_with_permutations_and_diagonals(oracle):
         p.plan(n, "fp32", fused=fused, fusion_width=3, tile_qubits=7)
         got = run_description(oracle, p.describe(), init.copy())
         assert np.max(np.abs(got - want)) < 1e-12
+
+
+def _required(qubit_lists, tables):
+    """Qubits every table holds whose 0 value makes every entry exactly 1."""
+    out = []
+    for q in qubit_lists[0]:
+        ok = True
+        for qs, tab in zip(qubit_lists, tables):
+            if q not in qs:
+                ok = False
+                break
+            i = qs.index(q)
+            for e, (re, im) in enumerate(tab):
+                if not (e >> i) & 1 and (re != 1.0 or im != 0.0):
+                    ok = False
+        if ok:
+            out.append(q)
+    return sorted(out)[:4]
+
+
+def _diag_programs():
+    rng = np.random.default_rng(12)
+    yield 14, circuits.qft(14)
+    yield 20, circuits.qft(20)
+    gs = []
+    for _ in range(40):  # CPHASE / CZ / RZ / dense mixes
+        a, b = (int(x) for x in rng.choice(16, 2, replace=False))
+        kind = int(rng.integers(4))
+        if kind == 0:
+            gs.append((gates.gate_matrix("CPHASE", float(rng.uniform(0.1, 3))), [a, b]))
+        elif kind == 1:
+            gs.append((gates.gate_matrix("CZ"), [a, b]))
+        elif kind == 2:
+            gs.append((gates.gate_matrix("RZ", float(rng.uniform(0.1, 3))), [a]))
+        else:
+            gs.append((gates.gate_matrix("H"), [a]))
+    yield 16, gs
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_plain_diagonal_required_qubits(prec):
+    """A plain diagonal pass visits only the amplitudes with its required
+    qubits set; the planner's choice equals a direct check of the tables."""
+    for n, gs in _diag_programs():
+        p = _program(gs)
+        p.plan(n, prec, fused=False)
+        for ps in p.describe()["passes"]:
+            if ps["kind"] != "diag":
+                continue
+            qls = [t["qubits"] for t in ps["tables"]]
+            tabs = [t["table"] for t in ps["tables"]]
+            assert ps["req"] == _required(qls, tabs), ps["req"]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_tile_diagonal_index_layout(prec):
+    """A diagonal op inside a tile pass reads its table index from the tile
+    index (runs of in-tile bits) and a per-tile constant (out-of-tile bits):
+    for random elements and tiles that equals gathering the index from the
+    global address; required bits match a direct check of the table."""
+    rng = np.random.default_rng(3)
+    for n, gs in _diag_programs():
+        p = _program(gs)
+        p.plan(n, prec, fused=True, fusion_width=2)
+        for ps in p.describe()["passes"]:
+            if ps["kind"] != "tile":
+                continue
+            t, L, E = ps["t"], ps["L"], ps["E"]
+            tile_of = {q: q for q in range(L)}
+            tile_of.update({q: L + e for e, q in enumerate(E)})
+            for op in ps["ops"]:
+                if op["kind"] != "diag":
+                    continue
+                pos, tpos = op["pos"], op["tpos"]
+                assert tpos == [tile_of.get(q, 255) for q in pos]
+                req = _required([pos], [op["data"]])
+                assert op["req_tile"] == sorted(tile_of[q] for q in req if q in tile_of)[:4]
+                assert op["out_req"] == sum(1 << pos.index(q) for q in req if q not in tile_of)
+                for _ in range(64):
+                    j = int(rng.integers(1 << t))
+                    g = int(rng.integers(1 << n))  # out-of-tile bits of the tile's base
+                    for b in range(t):            # the element's in-tile bits
+                        q = b if b < L else E[b - L]
+                        g = (g & ~(1 << q)) | (((j >> b) & 1) << q)
+                    want = sum(((g >> q) & 1) << i for i, q in enumerate(pos))
+                    got = sum(((g >> q) & 1) << i for i, q in enumerate(pos) if tpos[i] == 255)
+                    if op["nruns"] != 255:
+                        r = op["runs"]
+                        for k in range(0, len(r), 3):
+                            got |= ((j >> r[k]) & ((1 << r[k + 1]) - 1)) << r[k + 2]
+                    else:
+                        got |= sum(((j >> tp) & 1) << i for i, tp in enumerate(tpos) if tp != 255)
+                    assert got == want, (pos, tpos, op["runs"], j)
