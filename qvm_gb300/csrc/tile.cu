@@ -277,10 +277,27 @@ __device__ __forceinline__ unsigned diag_tile_element(const TileDiagInfo &di, un
   return u;
 }
 
+// Whether a thread's table index is the same for all its elements.  Thread
+// x takes elements u = x + k * blockDim (count and blockDim powers of two);
+// inserting the required bits is linear over disjoint bits, so its elements
+// differ only in the tile bits that the u bits at and above log2(blockDim)
+// land on.  If the table holds none of those bits, one lookup serves them all.
+__device__ __forceinline__ bool diag_thread_constant(const TileDiagInfo &di, const TileOpDev &op,
+                                                     unsigned count) {
+  const unsigned uvary = (count - 1u) & ~(blockDim.x - 1u);
+  const unsigned vmask = diag_tile_element(di, uvary) & ~diag_tile_element(di, 0u);
+  unsigned tmask = 0;
+  for (int i = 0; i < op.k; ++i)
+    if (di.tpos[i] != 255) tmask |= 1u << di.tpos[i];
+  return (tmask & vmask) == 0;
+}
+
 // Diagonal op: each element's table entry multiplies it (entries of 1 are
 // skipped).  The table is read in place from global memory through the
 // read-only cache: staging a pass's tables in shared memory (a QFT chain
-// takes up to 3 x 1024 entries) left room for one CTA per SM.
+// takes up to 3 x 1024 entries) left room for one CTA per SM.  Where a
+// thread's entry is the same for all its elements (two of the three tables
+// of a QFT chain), it is read once.
 template <typename T, bool S>
 __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
                                           const unsigned long long *rowoff, const TileOpDev &op,
@@ -290,6 +307,16 @@ __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
   const int cidx = diag_tile_const(di, op, rowoff);
   if (cidx < 0) return;
   const unsigned count = (1u << t) >> di.nreq;
+  if (threadIdx.x >= count) return;
+  if (diag_thread_constant(di, op, count)) {
+    const C ph = __ldg(table + diag_tile_index(di, op, cidx, diag_tile_element(di, threadIdx.x)));
+    if (ph.x == (T)1 && ph.y == (T)0) return;
+    for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+      const unsigned p = sw<S>(diag_tile_element(di, u));
+      tile[p] = cmul(tile[p], ph);
+    }
+    return;
+  }
   for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
     const unsigned j = diag_tile_element(di, u);
     const C ph = __ldg(table + diag_tile_index(di, op, cidx, j));
@@ -695,6 +722,18 @@ __device__ __forceinline__ void tile_diag_df(dfc *tile, int t, int L,
   const int cidx = diag_tile_const(di, op, rowoff);
   if (cidx < 0) return;
   const unsigned count = (1u << t) >> di.nreq;
+  if (threadIdx.x >= count) return;
+  if (diag_thread_constant(di, op, count)) {
+    const float4 e = __ldg(reinterpret_cast<const float4 *>(table) +
+                           diag_tile_index(di, op, cidx, diag_tile_element(di, threadIdx.x)));
+    if (e.x == 1.f && e.y == 0.f && e.z == 0.f && e.w == 0.f) return;
+    const dfc ph{e.x, e.y, e.z, e.w};
+    for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+      const unsigned p = sw<S>(diag_tile_element(di, u));
+      tile[p] = df_cmul(tile[p], ph);
+    }
+    return;
+  }
   for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
     const unsigned j = diag_tile_element(di, u);
     const float4 e =
