@@ -73,6 +73,49 @@ __device__ __forceinline__ int cut_value(unsigned long long x, const unsigned ch
   return c;
 }
 
+// The cut of x split by where each edge's endpoints lie against the 13-bit
+// tile (x = h << 13 | j): edges inside the low bits give a per-instance byte
+// table cl[j]; edges inside the high bits a constant per h; an edge between a
+// low qubit u and a high qubit v counts (j_u xor h_v).  The cross edges are
+// spread over up to kCutSlots slots, each low qubit at most once per slot, so
+// that their sum is popc((j ^ F_k) & M_k) over the slots: M_k the slot's low
+// qubits, F_k those whose high partner is 1 in h.
+constexpr int kCutSlots = 4;
+constexpr unsigned char kSlotLow = 255, kSlotHigh = 254;
+
+// F_k and the high-high count for high part h: warp-collective (all 32
+// lanes), every lane gets the results.
+__device__ __forceinline__ void cut_row(unsigned long long h, const unsigned char *e,
+                                        const unsigned char *slot, int m, unsigned *F, int &ch) {
+  const int lane = threadIdx.x & 31;
+  unsigned f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+  int c = 0;
+  for (int i = lane; i < m; i += 32) {
+    const int u = e[2 * i], v = e[2 * i + 1], sl = slot[i];
+    if (sl == kSlotHigh) {
+      c += (int)(((h >> (u - kQaoaTileBits)) ^ (h >> (v - kQaoaTileBits))) & 1ull);
+    } else if (sl < kCutSlots) {
+      const int lo = u < v ? u : v, hi = u < v ? v : u;
+      const unsigned bit = (unsigned)((h >> (hi - kQaoaTileBits)) & 1ull) << lo;
+      if (sl == 0) f0 |= bit;
+      else if (sl == 1) f1 |= bit;
+      else if (sl == 2) f2 |= bit;
+      else f3 |= bit;
+    }
+  }
+  F[0] = __reduce_or_sync(0xffffffffu, f0);
+  F[1] = __reduce_or_sync(0xffffffffu, f1);
+  F[2] = __reduce_or_sync(0xffffffffu, f2);
+  F[3] = __reduce_or_sync(0xffffffffu, f3);
+  ch = __reduce_add_sync(0xffffffffu, c);
+}
+
+__device__ __forceinline__ int cut_split(unsigned j, const unsigned char *cl, const unsigned *F,
+                                         const unsigned *M, int ch) {
+  return (int)cl[j] + ch + __popc((j ^ F[0]) & M[0]) + __popc((j ^ F[1]) & M[1]) +
+         __popc((j ^ F[2]) & M[2]) + __popc((j ^ F[3]) & M[3]);
+}
+
 __device__ __forceinline__ float2 rx_apply_lo(float2 a, float2 b, float c, float s) {
   // row 0 of [[c, -is], [-is, c]] * (a, b)
   return make_float2(c * a.x + s * b.y, c * a.y - s * b.x);
@@ -101,14 +144,18 @@ __device__ __forceinline__ double prob_d(float2 v) {
   return (double)v.x * (double)v.x + (double)v.y * (double)v.y;
 }
 
-__global__ void __launch_bounds__(kQaoaThreads) k_qaoa_batch(const __grid_constant__ QaoaArgs A) {
+__global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_constant__ QaoaArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *tile = reinterpret_cast<float2 *>(smem);                     // 2^13
   float2 *phase = tile + (1u << kQaoaTileBits);                         // kQaoaMaxEdges+1
   unsigned char *edges = reinterpret_cast<unsigned char *>(phase + kQaoaMaxEdges + 1);
+  unsigned char *cl = edges + 2 * kQaoaMaxEdges;                        // 2^13 low-edge cuts
   __shared__ double red[kQaoaThreads / 32];
   __shared__ int s_inst;
   __shared__ float s_c, s_s;
+  __shared__ unsigned char s_slot[kQaoaMaxEdges];
+  __shared__ unsigned s_M[kCutSlots], s_F[kCutSlots];
+  __shared__ int s_ch, s_split;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_inst = (int)atomicAdd(A.counter, 1u);
@@ -119,6 +166,40 @@ __global__ void __launch_bounds__(kQaoaThreads) k_qaoa_batch(const __grid_consta
     const int n = I.n, m = I.nedges;
     float2 *psi = A.states + I.state_off;
     for (int i = threadIdx.x; i < 2 * m; i += blockDim.x) edges[i] = A.edges[2 * I.edge_off + i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      // edge classes and cross-edge slots (the split cut; more than
+      // kCutSlots cross edges on one low qubit: the edge loop instead)
+      unsigned char cnt[kQaoaTileBits] = {};
+      unsigned M[kCutSlots] = {};
+      int ok = 1;
+      for (int i = 0; i < m; ++i) {
+        const int u = edges[2 * i], v = edges[2 * i + 1];
+        const bool ul = u < kQaoaTileBits, vl = v < kQaoaTileBits;
+        unsigned char sl = ul && vl ? kSlotLow : (!ul && !vl ? kSlotHigh : 0);
+        if (ul != vl) {
+          const int lo = ul ? u : v;
+          const int kk = cnt[lo]++;
+          if (kk >= kCutSlots) ok = 0;
+          else M[kk] |= 1u << lo;
+          sl = (unsigned char)(kk < kCutSlots ? kk : kSlotLow);
+        }
+        s_slot[i] = sl;
+      }
+      for (int k = 0; k < kCutSlots; ++k) s_M[k] = M[k];
+      s_split = ok;
+    }
+    __syncthreads();
+    const bool split = s_split != 0;
+    if (split) {
+      const unsigned nlow = 1u << (n < kQaoaTileBits ? n : kQaoaTileBits);
+      for (unsigned j = threadIdx.x; j < nlow; j += blockDim.x) {
+        int c = 0;
+        for (int i = 0; i < m; ++i)
+          if (s_slot[i] == kSlotLow) c += (int)(((j >> edges[2 * i]) ^ (j >> edges[2 * i + 1])) & 1u);
+        cl[j] = (unsigned char)c;
+      }
+    }
     const unsigned long long len = 1ull << n;
     const float amp0 = (float)(1.0 / sqrt((double)len));
     const bool resident = n <= kQaoaTileBits;
@@ -146,7 +227,7 @@ __global__ void __launch_bounds__(kQaoaThreads) k_qaoa_batch(const __grid_consta
       const float c = s_c, s = s_s;
       if (resident) {
         for (unsigned x = threadIdx.x; x < len; x += blockDim.x)
-          tile[x] = cmul(tile[x], phase[cut_value(x, edges, m)]);
+          tile[x] = cmul(tile[x], phase[split ? (int)cl[x] : cut_value(x, edges, m)]);
         __syncthreads();
         for (int q = 0; q < n; ++q) {
           tile_rx(tile, n, q, c, s);
@@ -161,9 +242,26 @@ __global__ void __launch_bounds__(kQaoaThreads) k_qaoa_batch(const __grid_consta
           __syncthreads();
           for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
             reinterpret_cast<float4 *>(tile)[j] = reinterpret_cast<const float4 *>(psi + base)[j];
+          if (split && threadIdx.x < 32) {
+            unsigned F[kCutSlots];
+            int ch;
+            cut_row(tcount, edges, s_slot, m, F, ch);
+            if (threadIdx.x == 0) {
+              for (int q = 0; q < kCutSlots; ++q) s_F[q] = F[q];
+              s_ch = ch;
+            }
+          }
           __syncthreads();
-          for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-            tile[j] = cmul(tile[j], phase[cut_value(base + j, edges, m)]);
+          if (split) {
+            const unsigned F[kCutSlots] = {s_F[0], s_F[1], s_F[2], s_F[3]};
+            const unsigned M[kCutSlots] = {s_M[0], s_M[1], s_M[2], s_M[3]};
+            const int ch = s_ch;
+            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
+              tile[j] = cmul(tile[j], phase[cut_split(j, cl, F, M, ch)]);
+          } else {
+            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
+              tile[j] = cmul(tile[j], phase[cut_value(base + j, edges, m)]);
+          }
           __syncthreads();
           for (int q = 0; q < tb; ++q) {
             tile_rx(tile, tb, q, c, s);
@@ -203,13 +301,21 @@ __global__ void __launch_bounds__(kQaoaThreads) k_qaoa_batch(const __grid_consta
     const unsigned long long nsub = len >> sbits;
     double *sub = A.subs + I.sub_off;
     double ex = 0.0;
+    const unsigned M[kCutSlots] = {s_M[0], s_M[1], s_M[2], s_M[3]};
     for (unsigned long long sb = warp; sb < nsub; sb += nwarps) {
       float hi = 0.f, lo = 0.f, exf = 0.f;
+      unsigned F[kCutSlots] = {0u, 0u, 0u, 0u};
+      int ch = 0;
+      // a sub-block (2^7 amplitudes) lies within one 2^13 row: one high part
+      if (split && !resident) cut_row((sb << sbits) >> kQaoaTileBits, edges, s_slot, m, F, ch);
       for (unsigned j = lane; j < (1u << sbits); j += 32) {
         unsigned long long x = (sb << sbits) + j;
         float2 v = psi[x];
         df_add_prob(hi, lo, v);  // exact squares for the CDF
-        exf = fmaf(fmaf(v.x, v.x, v.y * v.y), (float)cut_value(x, edges, m), exf);
+        const int cx = !split ? cut_value(x, edges, m)
+                       : resident ? (int)cl[x]
+                                  : cut_split((unsigned)(x & ((1u << kQaoaTileBits) - 1u)), cl, F, M, ch);
+        exf = fmaf(fmaf(v.x, v.x, v.y * v.y), (float)cx, exf);
       }
       double acc = warp_sum_d((double)hi + (double)lo);
       ex += (double)exf;
@@ -419,7 +525,8 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
   static std::once_flag attr_once;
   static cudaError_t attr_err = cudaSuccess;
   e = once(attr_once, attr_err, [] {
-    const int bytes = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges + 16;
+    const int bytes = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges +
+                      (1 << kQaoaTileBits) + 16;
     return cudaFuncSetAttribute(k_qaoa_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
   if (e != cudaSuccess) {
@@ -475,7 +582,8 @@ int qvmg_qaoa_batch_run(qvmg_qaoa_batch b, const double *draws, int nshots, doub
     cudaGraph_t g;
     QVMG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(b->counter, 0, sizeof(unsigned int), b->stream);
-    int smem = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges + 16;
+    int smem = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges +
+               (1 << kQaoaTileBits) + 16;
     int grid = std::min(b->ninst, sm_count() * 3);
     k_qaoa_batch<<<grid, kQaoaThreads, smem, b->stream>>>(A);
     cudaError_t le = cudaGetLastError();

@@ -49,3 +49,32 @@ def test_qaoa_batch_rerun_and_new_angles(gpu):
     e3, _ = b.run()
     assert not np.allclose(e1, e3)
     b.free()
+
+
+def test_qaoa_batch_cut_paths(gpu, oracle):
+    """The kernel splits each amplitude's cut into a low-bit table, a high-bit
+    constant and popcounts over cross-edge slots (at most 4 cross edges per
+    low qubit); a graph with more falls back to the edge loop.  Against the
+    oracle: split path -- qubit 0 with three cross edges (slots 0-2) beside
+    low-low and high-high edges (hub, 16 qubits), several low qubits with one
+    cross edge each (fan), a 15-qubit mix; fallback -- qubit 0 with five cross
+    edges (over, 18 qubits)."""
+    hub = (16, [(0, 13), (0, 14), (0, 15), (0, 12), (1, 13), (2, 3), (4, 14), (5, 15),
+                (13, 15), (6, 7), (0, 5)])
+    fan = (16, [(0, 13), (0, 14), (0, 15)] + [(1, 13), (2, 14), (3, 15)] + [(0, 12)])
+    mixed = (15, [(0, 13), (0, 14), (1, 13), (2, 14), (1, 2), (13, 14), (3, 12), (12, 13),
+                  (5, 6), (0, 5)])
+    # qubit 0 with 5 cross edges: n = 18 gives high qubits 13..17
+    over = (18, [(0, 13), (0, 14), (0, 15), (0, 16), (0, 17), (1, 2), (13, 17), (3, 16)])
+    graphs = [hub, fan, mixed, over]
+    rng = np.random.default_rng(5)
+    gam = [rng.uniform(0, np.pi, 2) for _ in graphs]
+    bet = [rng.uniform(0, np.pi / 2, 2) for _ in graphs]
+    b = QaoaBatch(graphs, gam, bet)
+    ex, _ = b.run(np.random.default_rng(6).random((len(graphs), 4)))
+    for i, (n, edges) in enumerate(graphs):
+        want = oracle_qaoa(oracle, n, edges, gam[i], bet[i])
+        assert np.max(np.abs(b.state(i) - want)) < 2e-6, (i, n)
+        wex = float(np.sum(np.abs(want) ** 2 * circuits.maxcut_values(n, edges)))
+        assert abs(ex[i] - wex) < 1e-5 * max(1.0, wex), (i, ex[i], wex)
+    b.free()
