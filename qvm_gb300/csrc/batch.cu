@@ -134,6 +134,39 @@ __device__ __forceinline__ void tile_rx(float2 *tile, int tb, int bit, float c, 
   }
 }
 
+// RX(2 beta) on local bits a < b in one sweep: each thread takes the four
+// amplitudes of a group, applies RX on bit a and then on bit b in registers
+// (the same operations, in the same order, as two single-bit sweeps).
+__device__ __forceinline__ void tile_rx2(float2 *tile, int tb, int a, int b, float c, float s) {
+  const unsigned ngroups = 1u << (tb - 2);
+  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
+    unsigned i = ((g >> a) << (a + 1)) | (g & ((1u << a) - 1u));
+    i = ((i >> b) << (b + 1)) | (i & ((1u << b) - 1u));
+    const unsigned ia = 1u << a, ib = 1u << b;
+    float2 v00 = tile[i], v01 = tile[i | ia], v10 = tile[i | ib], v11 = tile[i | ia | ib];
+    float2 w00 = rx_apply_lo(v00, v01, c, s), w01 = rx_apply_lo(v01, v00, c, s);
+    float2 w10 = rx_apply_lo(v10, v11, c, s), w11 = rx_apply_lo(v11, v10, c, s);
+    tile[i] = rx_apply_lo(w00, w10, c, s);
+    tile[i | ib] = rx_apply_lo(w10, w00, c, s);
+    tile[i | ia] = rx_apply_lo(w01, w11, c, s);
+    tile[i | ia | ib] = rx_apply_lo(w11, w01, c, s);
+  }
+}
+
+// RX on tile bits first .. first+count-1, two bits per sweep.
+__device__ __forceinline__ void tile_rx_run(float2 *tile, int tb, int first, int count, float c,
+                                            float s) {
+  int q = 0;
+  for (; q + 1 < count; q += 2) {
+    tile_rx2(tile, tb, first + q, first + q + 1, c, s);
+    __syncthreads();
+  }
+  if (q < count) {
+    tile_rx(tile, tb, first + q, c, s);
+    __syncthreads();
+  }
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -229,10 +262,7 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
         for (unsigned x = threadIdx.x; x < len; x += blockDim.x)
           tile[x] = cmul(tile[x], phase[split ? (int)cl[x] : cut_value(x, edges, m)]);
         __syncthreads();
-        for (int q = 0; q < n; ++q) {
-          tile_rx(tile, n, q, c, s);
-          __syncthreads();
-        }
+        tile_rx_run(tile, n, 0, n, c, s);
       } else {
         const int tb = kQaoaTileBits;
         const unsigned long long ntiles = len >> tb;
@@ -263,10 +293,7 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
               tile[j] = cmul(tile[j], phase[cut_value(base + j, edges, m)]);
           }
           __syncthreads();
-          for (int q = 0; q < tb; ++q) {
-            tile_rx(tile, tb, q, c, s);
-            __syncthreads();
-          }
+          tile_rx_run(tile, tb, 0, tb, c, s);
           for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
             reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
         }
@@ -279,10 +306,7 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
             tile[j] = psi[(h << tb) | (cidx << Lb) | lo];
           }
           __syncthreads();
-          for (int q = 0; q < hb; ++q) {
-            tile_rx(tile, tb, Lb + q, c, s);
-            __syncthreads();
-          }
+          tile_rx_run(tile, tb, Lb, hb, c, s);
           for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x) {
             unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
             psi[(h << tb) | (cidx << Lb) | lo] = tile[j];
