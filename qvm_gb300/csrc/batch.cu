@@ -18,6 +18,10 @@
 // ones stay in HBM and are swept in two tile passes per layer (low 13 qubits
 // contiguous; then the high qubits with a 2^(26-n)-amplitude row).  Amplitudes
 // are complex FP32; the phase table and RX coefficients are computed in FP64.
+// Each amplitude's cut comes from a per-instance table of the edges inside
+// the low 13 bits, a constant per row for the edges inside the high bits and
+// popcounts over the cross edges (cut_split); RX is applied two qubits per
+// shared-memory sweep.
 // All spin-free: the queue is a plain atomicAdd, no CTA waits on another.
 #include <cuda_runtime.h>
 #include <math.h>

@@ -13,12 +13,16 @@
 //    is applied entirely in registers -- fully unrolled complex FMAs with the
 //    block matrix held in registers, no shared-memory traffic and no address
 //    arithmetic per op;
-//  - shared-memory stages: diagonal phase tables (indexed by the global
-//    address), permutations, and dense blocks of 3..5 qubits, one group of
-//    2^k amplitudes per thread.
-// Shared memory is XOR-swizzled (bits 1..3 of a tile index are XORed with
-// bits 4..12 folded) so that the lanes of a warp spread over the banks in
-// both the row-contiguous copies and the register-stage gathers.
+//  - shared-memory stages: diagonal phase tables (read in place from global
+//    memory; each index from tile bits and per-tile constant bits as the
+//    planner laid out), permutations, and dense blocks, one group of 2^k
+//    amplitudes per thread (two groups sharing 16-byte words for FP32 1-/2-
+//    qubit blocks);
+//  - tensor-core stages: merged 3-/4-qubit blocks as tcgen05 MMAs.
+// In kernels with register stages shared memory is XOR-swizzled (bits 1..3
+// of a tile index are XORed with bits 4..12 folded) so that the lanes of a
+// warp spread over the banks in both the row-contiguous copies and the
+// register-stage gathers.
 // This is the GB300 form of the reference's per-gate complement iteration
 // (src/wavefunction.lisp:155-306, src/compile-gate.lisp:23-209): the same
 // gather -> matvec -> scatter, for many gates per HBM round trip.
