@@ -80,3 +80,20 @@ def test_priority_classes_give_identical_results(gpu):
             s.set_priority(2)
         finally:
             s.free()
+
+
+def test_device_reserve_and_out_of_memory(gpu):
+    """qvmg_device_reserve maps pool memory once; a reservation beyond the
+    device returns QVMG_E_NOMEM (after giving the pool's unused blocks back
+    and retrying), and states still allocate and compute afterwards."""
+    from qvm_gb300 import CudaPureState, _lib as L
+    assert L.lib().qvmg_device_reserve(1 << 30) == 0
+    assert L.lib().qvmg_device_reserve(1 << 50) == 3  # QVMG_E_NOMEM
+    s = CudaPureState(26, "fp64")
+    try:
+        from qvm_gb300 import gates as G
+        s.apply_matrix(G.gate_matrix("H"), [25])
+        assert abs(s.excited_probability(25) - 0.5) < 1e-12
+        assert abs(s.norm() - 1.0) < 1e-12
+    finally:
+        s.free()
