@@ -84,8 +84,9 @@ int qvmg_device_info(int *sm_count, uint64_t *free_bytes, uint64_t *total_bytes)
 /* Grow the device memory pool that states, scratch and plans come from by
  * `bytes` (in blocks of up to 16 GiB) and keep it: later allocations need no
  * new mapping, which can stall other threads' CUDA calls while the GPU is
- * busy.  A server calls it once with its HBM budget; QVMG_E_NOMEM if the
- * device cannot hold it (what was reserved stays in the pool). */
+ * busy.  A server calls it once with its HBM budget.  QVMG_E_NOMEM if the
+ * device cannot hold it; then nothing stays reserved (the pool's unused memory
+ * is returned to the device). */
 int qvmg_device_reserve(uint64_t bytes);
 /* HBM bytes a state of this size and precision holds (16*2^n or 8*2^n plus
  * its reduction scratch); 0 for invalid arguments. */

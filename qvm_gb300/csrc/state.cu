@@ -420,7 +420,15 @@ int qvmg_device_reserve(uint64_t bytes) {
   }
   for (void *p : got) dev_free(p, st);
   cudaError_t e = cudaStreamSynchronize(st);
-  if (rc) return rc;
+  if (rc) {
+    // a failed reservation keeps nothing: the pool's unused memory goes back
+    // to the device, so that other allocators in the process still find it
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+      cudaMemPoolTrimTo(pool, 0);
+    return rc;
+  }
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
   return QVMG_OK;
 }

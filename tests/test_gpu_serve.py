@@ -84,8 +84,9 @@ def test_priority_classes_give_identical_results(gpu):
 
 def test_device_reserve_and_out_of_memory(gpu):
     """qvmg_device_reserve maps pool memory once; a reservation beyond the
-    device returns QVMG_E_NOMEM (after giving the pool's unused blocks back
-    and retrying), and states still allocate and compute afterwards."""
+    device returns QVMG_E_NOMEM and keeps nothing (the pool's unused memory
+    goes back to the device), and states still allocate and compute
+    afterwards."""
     from qvm_gb300 import CudaPureState, _lib as L
     assert L.lib().qvmg_device_reserve(1 << 30) == 0
     assert L.lib().qvmg_device_reserve(1 << 50) == 3  # QVMG_E_NOMEM
