@@ -193,6 +193,8 @@ class Server:
                 s.free()
             if item is None:
                 if evicted and not self.stop:
+                    with self.cv:  # budget was freed: other lanes may admit now
+                        self.cv.notify_all()
                     continue
                 return
             req, fut, need, st = item
