@@ -101,15 +101,17 @@ class StatePool:
 
 class Server:
     def __init__(self, hbm_budget: float = 180e9, workers: int = 16, aging_s: float = 2.0,
-                 fast_workers: int = 8, fast_cost: float = 1000.0 * (1 << 24)):
+                 fast_workers: int = 8, fast_cost: float = 1000.0 * (1 << 24),
+                 reserve_pool: bool = True):
         """`workers` take any request; `fast_workers` more take only requests
         whose estimated cost (gates x 2^n, FP64 x 8) is at most `fast_cost`
         (by default a 1000-gate 24-qubit FP32 program), so that a small
-        request never waits for a worker held by a multi-second job."""
+        request never waits for a worker held by a multi-second job.
+        `reserve_pool` maps the budget into the device memory pool at start."""
         self.budget = int(hbm_budget)
         self.aging_s = float(aging_s)
         self.fast_cost = float(fast_cost)
-        if workers + fast_workers > 0:
+        if reserve_pool and workers + fast_workers > 0:
             # map the budget's device memory once: growing the pool while
             # requests run stalls the workers' CUDA calls
             from . import _lib as L

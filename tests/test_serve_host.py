@@ -52,3 +52,83 @@ def test_budget_holds_back_what_does_not_fit():
     assert srv._admit() is not None
     assert srv._admit() is None          # the second does not fit beside the first
     assert srv.reserved <= srv.budget
+
+
+class _FakeState:
+    """Stands in for a device state: tracks live bytes, records priorities."""
+    lock = None
+    live = 0
+    peak = 0
+
+    def __init__(self, n, prec):
+        self.n, self.prec, self.prio = n, prec, 0
+        with _FakeState.lock:
+            _FakeState.live += state_bytes(n, prec)
+            _FakeState.peak = max(_FakeState.peak, _FakeState.live)
+
+    def num_qubits(self):
+        return self.n
+
+    def set_to_zero_state(self):
+        pass
+
+    def set_priority(self, p):
+        self.prio = p
+
+    def sample(self, draws):
+        time.sleep(0.002)
+        return np.floor(np.asarray(draws) * (1 << self.n)).astype(np.int64) * 2 + (self.prio > 0)
+
+    def free(self):
+        with _FakeState.lock:
+            _FakeState.live -= state_bytes(self.n, self.prec)
+
+
+class _FakeProgram:
+    def add_gates(self, gates):
+        self.ng = len(gates)
+        return self
+
+    def plan(self, *a, **k):
+        pass
+
+    def run(self, st, fused=True):
+        time.sleep(0.001 * (1 + st.n % 3))
+
+    def free(self):
+        pass
+
+
+def test_workers_lanes_eviction_and_priority(monkeypatch):
+    """The worker loop with fake states: every request completes with its
+    own result, cheap ones on the fast lane's high priority and the others
+    yielding, pooled states are evicted within the budget."""
+    import threading
+    from qvm_gb300 import serve
+    monkeypatch.setattr(serve, "CudaPureState", _FakeState)
+    monkeypatch.setattr(serve, "Program", _FakeProgram)
+    _FakeState.lock = threading.Lock()
+    _FakeState.live = _FakeState.peak = 0
+    budget = 3 * state_bytes(20, "fp64")
+    fast_cost = 200.0 * (1 << 14)
+    srv = Server(hbm_budget=budget, workers=3, fast_workers=2, fast_cost=fast_cost,
+                 reserve_pool=False)
+    rng = np.random.default_rng(8)
+    reqs = []
+    for i in range(60):
+        n = int(rng.choice([10, 12, 14, 18, 20]))
+        prec = "fp32" if i % 2 else "fp64"
+        gates = [None] * int(rng.integers(5, 300))
+        reqs.append(Request(n, gates, 16, prec, rng.random(16), True, f"r{i}"))
+    futs = [(r, srv.submit(r)) for r in reqs]
+    for r, f in futs:
+        res = f.result(timeout=60)
+        high = Server.cost(r) <= fast_cost
+        want = np.floor(r.draws * (1 << r.n)).astype(np.int64) * 2 + int(high)
+        np.testing.assert_array_equal(res.shots, want)
+    assert srv.reserved <= budget
+    srv.close()
+    assert _FakeState.live == 0                      # everything freed at close
+    # evicted states are freed outside the lock, so new states may briefly
+    # overlap them: at most one evicted state per worker (5) beyond the budget
+    assert _FakeState.peak <= budget + 5 * state_bytes(20, "fp64")
