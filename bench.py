@@ -4,16 +4,20 @@
 One step = reset a 30-qubit state to |0...0> and run the whole 900-gate
 circuit (per layer: a Haar SU(2) on every qubit, then a Haar SU(4) on each
 pair of a random perfect matching; seeded synthetic input) through the fused
-FP32 path, state resident in HBM.  The line also reports the plain FP64 path
-on the same circuit, the fused-FP32 vs FP64 fidelity and max amplitude
-error, 4096 shots sampled from both states with the same uniform draws, the
-tile kernel's roofline, an end-to-end number through the public API with
-host buffers, and a CPU baseline (the oracle restatement of the reference's
-per-gate algorithm on the host cores).
+FP32 path, state resident in HBM.  The line also reports the plain FP64
+kernels and the fused double-float FP64 tiles on the same circuit, the
+fused-FP32 vs FP64 fidelity and max amplitude error, 4096 shots sampled from
+both states with the same uniform draws, the tile kernel's roofline, an
+end-to-end number through the public API with host buffers, a CPU baseline
+(the oracle restatement of the reference's per-gate algorithm on the host
+cores, FP64) and the precision-matched ratios against it, plus the other
+workloads (32-qubit circuit, 28-qubit FP64 QFT, batched QAOA, serving, ...).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 Under torchrun each rank runs an independent replica on its own GPU
 (the workload does not shard); value = all ranks' gates / max rank time.
+With --impl reference, one step is a fixed 15-gate sample of the circuit
+(a third of a layer, the layer's gate mix) on the CPU port, FP64.
 """
 from __future__ import annotations
 
@@ -63,7 +67,10 @@ def parse():
                     help="skip the per-kind timing of memory-bound plain passes")
     ap.add_argument("--no-layers", action="store_true",
                     help="skip the 20-qubit layer circuit with 1000 shots")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-steps", type=int, default=3,
+                    help="timed samples of the CPU baseline (about 6 s each at 30 qubits)")
+    ap.add_argument("--no-32q-plain", action="store_true",
+                    help="skip the plain FP64 kernels at 32 qubits (about 80 s)")
     return ap.parse_args()
 
 
@@ -166,24 +173,44 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n, gates, seconds, threads):
+def reference_sample(gates, n, j):
+    """The j-th fixed CPU-timing sample of the circuit: one third of layer
+    (j // 3) mod depth, part r = j % 3 -- that layer's SU(2)s on the r-th
+    third of the qubits followed by the r-th third of its SU(4)s (for 30
+    qubits 10 SU(2) + 5 SU(4), the same 2:1 mix as a whole layer), in circuit
+    order.  Used by the reference arm and the CPU baseline alike."""
+    per_layer = n + n // 2
+    depth = len(gates) // per_layer
+    layer = (j // 3) % depth
+    r = j % 3
+    base = layer * per_layer
+    one = np.array_split(np.arange(n), 3)[r]
+    two = np.array_split(np.arange(n // 2), 3)[r]
+    return [gates[base + int(i)] for i in one] + [gates[base + n + int(i)] for i in two]
+
+
+def cpu_baseline(n, gates, steps, threads):
     """The oracle (restatement of the reference's per-gate apply-matrix-
-    operator with worker-parallel loops) on the host cores: a bounded sample
-    of the same circuit -- its first gates, until `seconds` have passed."""
+    operator with worker-parallel loops) on the host cores: one untimed
+    sample, then `steps` timed samples of the circuit (reference_sample),
+    applied in turn to one FP64 state."""
     from oracle import oracle as O
     O.set_workers(threads, threshold=19)
     wf = O.zero_state(n)
-    t0 = time.perf_counter()
-    done = 0
-    for m, qs in gates:
+    for m, qs in reference_sample(gates, n, 0):
         O.apply_matrix_operator(wf, m, qs)
-        done += 1
-        if time.perf_counter() - t0 > seconds:
-            break
-    dt = time.perf_counter() - t0
+    done, dt = 0, 0.0
+    for j in range(1, steps + 1):
+        sample = reference_sample(gates, n, j)
+        t0 = time.perf_counter()
+        for m, qs in sample:
+            O.apply_matrix_operator(wf, m, qs)
+        dt += time.perf_counter() - t0
+        done += len(sample)
     del wf
     return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {done} of {len(gates)} gates of the {n}-qubit circuit, FP64, "
+            "sample": f"{steps} samples of {done // steps} gates (one third of a layer: "
+                      f"{n // 3} SU(2) + {n // 6} SU(4)) of the {n}-qubit circuit, FP64, "
                       f"{dt:.1f} s"}
 
 
@@ -477,13 +504,12 @@ def run_endpoints(n: int = 26, seed: int = 7):
 
 
 def run_random32(fw: int, tile: int, engine: str, shots: int = 4096, seed: int = 3,
-                 runs: int = 3):
+                 runs: int = 3, plain: bool = True):
     """The random circuit at 32 qubits (depth 20, 960 gates): fused FP32
-    (32 GiB state) with the tuned engine and with the tensor-core engine,
-    against fused FP64 (64 GiB state; double-float tiles, within 1e-13 of the
-    plain FP64 kernels).  The plain FP64 kernels would take ~80 s here and
-    are timed at 30 qubits instead.  Fidelity, max amplitude error and the
-    shots drawn from the same uniforms are reported."""
+    (32 GiB state) with the tuned engine and with the tensor-core engine;
+    fused FP64 in double-float tiles and the plain FP64 kernels (64 GiB
+    states each).  Fidelity and max amplitude error of the tuned FP32 state
+    against plain FP64, and the shots both draw from the same 4096 uniforms."""
     from qvm_gb300 import CudaPureState, Program, circuits
     from qvm_gb300.autotune import apply_engine
     n = 32
@@ -492,6 +518,8 @@ def run_random32(fw: int, tile: int, engine: str, shots: int = 4096, seed: int =
     s32 = CudaPureState(n, "fp32")
     out = {"workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth 20, {G} gates"}
     for label, (f, t, e) in (("fp32_" + engine, (fw, tile, engine)), ("fp32_tc", (4, 13, "tc"))):
+        if label == "fp32_tc" and engine == "tc":
+            continue
         prog = Program()
         prog.add_gates(gates)
         apply_engine(prog, e)
@@ -504,29 +532,42 @@ def run_random32(fw: int, tile: int, engine: str, shots: int = 4096, seed: int =
         out[label] = {"ms": best, "gates_per_s": G / (best / 1e3), "fusion_width": f,
                       "tile_qubits": t}
         prog.free()
-    s64 = CudaPureState(n, "fp64")
+    sdf = CudaPureState(n, "fp64")
     prog = Program()
     prog.add_gates(gates)
     prog.plan(n, "fp64", fused=True, fusion_width=2, tile_qubits=12)
     t0 = time.perf_counter()
-    prog.run(s64, fused=True)
-    s64.sync()
-    out["fp64_fused_ms"] = 1e3 * (time.perf_counter() - t0)
+    prog.run(sdf, fused=True)
+    sdf.sync()
+    out["fused_df64"] = {"ms": 1e3 * (time.perf_counter() - t0)}
+    out["fused_df64"]["gates_per_s"] = G / (out["fused_df64"]["ms"] / 1e3)
+    ref, ref_name = sdf, "fused FP64 (double-float tiles)"
+    if plain:
+        sp = CudaPureState(n, "fp64")
+        t0 = time.perf_counter()
+        prog.run(sp, fused=False)
+        sp.sync()
+        ms_p = 1e3 * (time.perf_counter() - t0)
+        fdf, edf = sp.fidelity(sdf)
+        out["plain_fp64"] = {"ms": ms_p, "gates_per_s": G / (ms_p / 1e3)}
+        out["fused_df64"].update({"fidelity_vs_plain_fp64": fdf, "max_abs_err": edf})
+        sdf.free()
+        ref, ref_name = sp, "plain FP64 kernels"
     prog.free()
-    # the state of the tuned FP32 engine against it
+    # the state of the tuned FP32 engine against the FP64 reference state
     prog = Program()
     prog.add_gates(gates)
     apply_engine(prog, engine)
     prog.plan(n, "fp32", fused=True, fusion_width=fw, tile_qubits=tile)
     s32.set_to_zero_state()
     prog.run(s32, fused=True)
-    f, err = s64.fidelity(s32)
+    f, err = ref.fidelity(s32)
     draws = np.random.default_rng(seed + 1).random(shots)
-    same = int((s64.sample(draws) == s32.sample(draws)).sum())
-    out["fidelity"] = {"fused_fp32_vs_fp64": f, "max_abs_err": err, "shots": shots,
-                       "identical_shots": same}
+    same = int((ref.sample(draws) == s32.sample(draws)).sum())
+    out["fidelity"] = {"fused_fp32_vs": ref_name, "fidelity": f, "one_minus": 1.0 - f,
+                       "max_abs_err": err, "shots": shots, "identical_shots": same}
     prog.free()
-    s64.free()
+    ref.free()
     s32.free()
     return out
 
@@ -569,29 +610,47 @@ def run_serving(arrive_s: float = 1.5, drain_s: float = 60.0, seed: int = 5):
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the reference's CPU algorithm
+    (no SBCL here), all host cores, FP64.  One step = one fixed sample of the
+    circuit (reference_sample: a third of a layer, 15 gates at 30 qubits,
+    the layer's gate mix), applied in turn to one state; ms_per_step is the
+    measured time of those steps."""
     ws, rank, _ = dist()
     if rank != 0:
         return
+    from oracle import oracle as O
     from qvm_gb300 import circuits
-    gates = circuits.random_su_circuit(args.n, args.depth, args.seed)
+    n = args.n
+    gates = circuits.random_su_circuit(n, args.depth, args.seed)
     threads = os.cpu_count() or 1
-    per_step = max(2.0, min(args.cpu_seconds, 20.0))
-    vals = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline(args.n, gates, per_step if i >= args.warmup else 1.0, threads)
-        if i >= args.warmup:
-            vals.append(r)
-    value = float(np.mean([v["value"] for v in vals]))
+    O.set_workers(threads, threshold=19)
+    wf = O.zero_state(n)
+    step_ms, done = [], 0
+    for j in range(args.warmup + args.steps):
+        sample = reference_sample(gates, n, j)
+        t0 = time.perf_counter()
+        for m, qs in sample:
+            O.apply_matrix_operator(wf, m, qs)
+        dt = time.perf_counter() - t0
+        if j >= args.warmup:
+            step_ms.append(1e3 * dt)
+            done += len(sample)
+    total_ms = float(np.sum(step_ms))
+    value = done / (total_ms / 1e3)
+    per = done // args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * len(gates) / value,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Haar SU(2)/SU(4) circuit)", "impl": "reference",
-            "config": {"workload": f"random SU(2)/SU(4) circuit, {args.n} qubits, depth "
-                                   f"{args.depth}, {len(gates)} gates",
+            "config": {"workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth "
+                                   f"{args.depth}; one step = {per} of its gates (a third "
+                                   f"of a layer: {n // 3} SU(2) + {n // 6} SU(4)), FP64, "
+                                   f"applied in circuit order to one state",
                        "cpu": "oracle restatement of the reference's apply-matrix-operator "
                               "(no SBCL on this host)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": vals[-1]["sample"]},
+                             "sample": f"{args.steps} timed steps of {per} gates, "
+                                       f"{total_ms / 1e3:.1f} s"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -716,12 +775,13 @@ def main():
                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                      "what": "Program build + plan + upload + run + 4096 shots via the C ABI"}
 
-    # --- plain FP64 comparison, fidelity, shots --------------------------------------
+    # --- plain FP64 and fused double-float FP64, fidelity, shots --------------------
     if not args.no_fp64 and rank == 0:
         s64 = CudaPureState(n, "fp64")
         pp = Program()
         pp.add_gates(gates[:8])
         pp.run(s64, fused=False)       # warm-up on a prefix
+        pp.free()
         s64.set_to_zero_state()
         s64.sync()
         st64 = torch.cuda.ExternalStream(s64.stream())
@@ -732,21 +792,38 @@ def main():
         b.record(st64)
         b.synchronize()
         ms64 = a.elapsed_time(b)
+        # the same circuit in fused double-float tiles (FP64 state in HBM)
+        pf = Program()
+        pf.add_gates(gates)
+        pf.plan(n, "fp64", fused=True, fusion_width=2, tile_qubits=12)
+        sdf = CudaPureState(n, "fp64")
+        pf.run(sdf, fused=True)        # untimed: plan upload
+        dfbest = float("inf")
+        for _ in range(2):
+            sdf.set_to_zero_state()
+            ms_df, _ = pf.run_profiled(sdf, fused=True)
+            dfbest = min(dfbest, float(ms_df.sum()))
+        fdf, errdf = s64.fidelity(sdf)
+        sdf.free()
+        pf.free()
         s32.set_to_zero_state()
         prog.run(s32, fused=True)
         f, err = s64.fidelity(s32)
         sh64 = s64.sample(draws)
         sh32 = s32.sample(draws)
-        result["plain_fp64"] = {"gates_per_s": G / (ms64 / 1e3), "ms": ms64,
-                                "speedup_fused_fp32": (G / (ms64 / 1e3)) and value / ws /
-                                (G / (ms64 / 1e3))}
-        result["fidelity"] = {"fused_fp32_vs_fp64": f, "max_abs_err": err,
-                              "shots": int(args.shots),
+        g64 = G / (ms64 / 1e3)
+        result["plain_fp64"] = {"gates_per_s": g64, "ms": ms64,
+                                "speedup_fused_fp32": value / ws / g64}
+        result["fused_df64"] = {"gates_per_s": G / (dfbest / 1e3), "ms": dfbest,
+                                "fidelity_vs_plain_fp64": fdf, "max_abs_err": errdf}
+        result["fidelity"] = {"fused_fp32_vs_fp64": f, "one_minus": 1.0 - f,
+                              "max_abs_err": err, "shots": int(args.shots),
                               "identical_shots": int((sh64 == sh32).sum())}
         s64.free()
     if not args.no_32q and rank == 0:
-        s32.free()  # 8 GiB back before the 32 + 64 GiB states
-        result["random32"] = run_random32(args.fw, args.tile, args.engine)
+        s32.free()  # 8 GiB back before the 32-qubit states
+        result["random32"] = run_random32(args.fw, args.tile, args.engine,
+                                          plain=not args.no_32q_plain)
         s32 = CudaPureState(n, "fp32")
     if not args.no_qft and rank == 0:
         result[f"qft{args.qft_n}_fp64"] = run_qft_fp64(args.qft_n)
@@ -760,13 +837,55 @@ def main():
         result["batch_qaoa"] = run_qaoa_batch()
     if not args.no_serve and rank == 0:
         result["serving"] = run_serving()
-    if not args.no_cpu and rank == 0:
-        result["cpu_baseline"] = cpu_baseline(n, gates, args.cpu_seconds, os.cpu_count() or 1)
+    if not args.no_cpu and rank == 0 and ws == 1:
+        cb = cpu_baseline(n, gates, args.cpu_steps, os.cpu_count() or 1)
+        result["cpu_baseline"] = cb
+        if "plain_fp64" in result:
+            # precision-matched: FP64 on the GPU against the FP64 CPU port
+            result["same_precision"] = {
+                "cpu_fp64_gates_per_s": cb["value"],
+                "plain_fp64_gates_per_s": result["plain_fp64"]["gates_per_s"],
+                "fused_df64_gates_per_s": result["fused_df64"]["gates_per_s"],
+                "plain_fp64_vs_cpu": result["plain_fp64"]["gates_per_s"] / cb["value"],
+                "fused_df64_vs_cpu": result["fused_df64"]["gates_per_s"] / cb["value"],
+                "fused_fp32_vs_cpu": value / ws / cb["value"]}
     if rank == 0:
-        print(json.dumps(result), flush=True)
+        print(json.dumps(ordered(result)), flush=True)
     s32.free()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+# Keys of the bench line, in print order: the contract's keys, then the
+# detailed legs, then the summary figures last (a reader of only the end of
+# the line still sees them).
+_LEAD = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+         "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "gpu_launches",
+         "config", "roofline", "clocks", "e2e", "cpu_baseline")
+_TAIL = ("latency_ms", "random32", "qft28_fp64", "same_precision", "fused_df64", "plain_fp64",
+         "fidelity")
+
+
+def _round(x, digits=5):
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}") if np.isfinite(x) else x
+    if isinstance(x, dict):
+        return {k: _round(v, digits) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_round(v, digits) for v in x]
+    return x
+
+
+def ordered(result):
+    out = {k: result[k] for k in _LEAD if k in result}
+    middle = [k for k in result if k not in _LEAD and k not in _TAIL]
+    for k in middle:
+        out[k] = _round(result[k])
+    for k in _TAIL:
+        if k in result:
+            # fidelities keep full precision; the other figures 5 digits
+            out[k] = result[k] if k in ("fidelity", "fused_df64") else _round(result[k])
+    return out
 
 
 if __name__ == "__main__":

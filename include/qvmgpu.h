@@ -88,6 +88,11 @@ int qvmg_device_info(int *sm_count, uint64_t *free_bytes, uint64_t *total_bytes)
  * device cannot hold it; then nothing stays reserved (the pool's unused memory
  * is returned to the device). */
 int qvmg_device_reserve(uint64_t bytes);
+/* Test hook (no counterpart in the reference, which has no device memory):
+ * the `nth` device allocation the library makes from now on (1 = the next)
+ * fails with QVMG_E_NOMEM without reaching CUDA; 0 cancels.  Lets host-side
+ * tests drive the out-of-memory paths without exhausting a shared GPU. */
+int qvmg_debug_fail_alloc(int nth);
 /* HBM bytes a state of this size and precision holds (16*2^n or 8*2^n plus
  * its reduction scratch); 0 for invalid arguments. */
 uint64_t qvmg_state_bytes(int nqubits, int precision);

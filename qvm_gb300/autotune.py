@@ -6,7 +6,9 @@ the per-pass CUDA events of ``Program.run_profiled``, and keeps the fastest.
 Engines of an FP32 tile: "fma" (every block through shared memory on FP32
 FMAs), "reg" (runs of 1-/2-qubit blocks on amplitudes held in registers) and
 "tc" (blocks merged to 3-4 qubits and run as tcgen05 TF32 MMAs).
-Results are cached in memory per (program id, qubits, precision).
+Results are cached on the Program object itself, per (qubits, precision,
+candidate list, op-list generation): a freed program's choice can never be
+served to a new one, and adding ops to a program retunes it.
 """
 from __future__ import annotations
 
@@ -22,8 +24,6 @@ DEFAULT_CANDIDATES = {
     "fp64": [(fw, t, "fma") for fw in (1, 2, 3) for t in (11, 12, 13)],
 }
 
-_cache: dict = {}
-
 
 def apply_engine(prog: Program, engine: str):
     prog.set_register_stages(engine == "reg")
@@ -36,11 +36,16 @@ def autotune(prog: Program, state: CudaPureState, precision: str = "fp32", candi
     returns (best, table) with table[candidate] = device ms per run.  The
     state is overwritten (it is reset before every trial)."""
     n = state.num_qubits()
-    key = (id(prog), n, precision)
-    if key in _cache:
-        return _cache[key]
+    cands = tuple(candidates or DEFAULT_CANDIDATES[precision])
+    cache = prog.__dict__.setdefault("_autotune_cache", {})
+    key = (n, precision, cands, prog.generation)
+    if key in cache:
+        choice, table = cache[key]
+        apply_engine(prog, choice[2])
+        prog.plan(n, precision, fused=True, fusion_width=choice[0], tile_qubits=choice[1])
+        return choice, table
     table = {}
-    for fw, tile, engine in candidates or DEFAULT_CANDIDATES[precision]:
+    for fw, tile, engine in cands:
         try:
             apply_engine(prog, engine)
             prog.plan(n, precision, fused=True, fusion_width=fw, tile_qubits=tile)
@@ -55,5 +60,5 @@ def autotune(prog: Program, state: CudaPureState, precision: str = "fp32", candi
     choice = min(table, key=table.get)
     apply_engine(prog, choice[2])
     prog.plan(n, precision, fused=True, fusion_width=choice[0], tile_qubits=choice[1])
-    _cache[key] = (choice, table)
+    cache[key] = (choice, table)
     return choice, table

@@ -581,17 +581,35 @@ int qvmg_qaoa_batch_run(qvmg_qaoa_batch b, const double *draws, int nshots, doub
     return fail(QVMG_E_INVALID, "shots requested without draws or output");
   if (nshots > b->nshots_cap) {
     QVMG_CUDA(cudaStreamSynchronize(b->stream));
-    cudaFree(b->draws);
-    cudaFree(b->shots);
-    b->draws = nullptr;
-    b->shots = nullptr;
-    QVMG_CUDA(cudaMalloc(&b->draws, sizeof(double) * (size_t)b->ninst * nshots));
-    QVMG_CUDA(cudaMalloc(&b->shots, sizeof(unsigned int) * (size_t)b->ninst * nshots));
-    b->nshots_cap = nshots;
+    // The cached graph holds the old buffers: drop it before they are freed,
+    // and record the capacity only once both new buffers exist, so that a
+    // failed allocation can never leave a graph that writes freed memory.
     if (b->graph) {
       cudaGraphExecDestroy(b->graph);
       b->graph = nullptr;
     }
+    b->graph_shots = -1;
+    cudaFree(b->draws);
+    cudaFree(b->shots);
+    b->draws = nullptr;
+    b->shots = nullptr;
+    b->nshots_cap = 0;
+    void *d = nullptr, *sh = nullptr;
+    cudaError_t e = alloc_fault_injected() ? cudaErrorMemoryAllocation
+                                           : cudaMalloc(&d, sizeof(double) * (size_t)b->ninst * nshots);
+    if (e == cudaSuccess)
+      e = alloc_fault_injected()
+              ? cudaErrorMemoryAllocation
+              : cudaMalloc(&sh, sizeof(unsigned int) * (size_t)b->ninst * nshots);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      cudaFree(sh);
+      cudaGetLastError();
+      return cuda_fail(e, "cudaMalloc(batch draws and shots)");
+    }
+    b->draws = (double *)d;
+    b->shots = (unsigned int *)sh;
+    b->nshots_cap = nshots;
   }
   QaoaArgs &A = b->args;
   A.nshots = nshots;

@@ -88,6 +88,9 @@ int sm_count();
 // serving engine stalled every worker until all queued passes had drained.
 // The device's default pool keeps freed memory for reuse.
 int dev_alloc(void **p, size_t bytes, cudaStream_t s);
+// True when the test hook qvmg_debug_fail_alloc asks this allocation to
+// fail; every device allocation of the library consults it once.
+bool alloc_fault_injected();
 void dev_free(void *p, cudaStream_t s);
 // A library stream for frees that must wait on other streams' events.
 cudaStream_t free_stream();

@@ -13,6 +13,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <thread>
 #include <mutex>
@@ -81,29 +82,51 @@ int check_qubits(qvmg_state s, int k, const int *qubits, int kmax) {
   return QVMG_OK;
 }
 
+// Test hook: the nth device allocation from now fails as out of memory.
+static std::atomic<int> g_alloc_fault_countdown{0};
+
+bool alloc_fault_injected() {
+  int c = g_alloc_fault_countdown.load();
+  while (c > 0) {
+    if (g_alloc_fault_countdown.compare_exchange_weak(c, c - 1)) return c == 1;
+  }
+  return false;
+}
+
 int dev_alloc(void **p, size_t bytes, cudaStream_t s) {
-  static std::once_flag flag;
-  static cudaError_t err = cudaSuccess;
-  QVMG_CUDA(once(flag, err, [] {
-    // keep freed memory in the pool: states and plans come and go per request
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+  // Keep freed memory in each device's pool: states and plans come and go
+  // per request.  The release threshold is a per-pool setting, so it is set
+  // once for every device the library allocates on.
+  constexpr int kMaxDevices = 64;
+  static std::once_flag flags[kMaxDevices];
+  static cudaError_t errs[kMaxDevices];
+  int dev = 0;
+  QVMG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(QVMG_E_INVALID, "device ordinal out of range");
+  QVMG_CUDA(once(flags[dev], errs[dev], [dev] {
     cudaMemPool_t pool;
-    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, dev);
     uint64_t keep = ~0ull;
     if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     return e;
   }));
+  if (alloc_fault_injected()) {
+    *p = nullptr;
+    return fail(QVMG_E_NOMEM, "injected device allocation failure (qvmg_debug_fail_alloc)");
+  }
   cudaError_t e = cudaMallocAsync(p, bytes, s);
   if (e == cudaErrorMemoryAllocation) {
     // The pool keeps freed blocks; if none is large enough and the device is
-    // full, give the unused ones back (after the frees queued so far) and
-    // retry once.
+    // full, give the unused ones back and retry once.  Only the allocating
+    // stream and the library's free stream are waited for (their queued
+    // frees land in the pool): a device-wide synchronize would also break
+    // a graph capture running on another thread.
     cudaGetLastError();
-    int dev = 0;
     cudaMemPool_t pool;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess &&
-        cudaDeviceSynchronize() == cudaSuccess && cudaMemPoolTrimTo(pool, 0) == cudaSuccess)
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess &&
+        cudaStreamSynchronize(s) == cudaSuccess &&
+        cudaStreamSynchronize(free_stream()) == cudaSuccess &&
+        cudaMemPoolTrimTo(pool, 0) == cudaSuccess)
       e = cudaMallocAsync(p, bytes, s);
   }
   if (e != cudaSuccess) {
@@ -314,6 +337,12 @@ extern "C" {
 const char *qvmg_last_error(void) { return g_last_error.c_str(); }
 
 int qvmg_abi_version(void) { return QVMG_ABI_VERSION; }
+
+int qvmg_debug_fail_alloc(int nth) {
+  if (nth < 0) return fail(QVMG_E_INVALID, "negative allocation countdown");
+  g_alloc_fault_countdown.store(nth);
+  return QVMG_OK;
+}
 
 int qvmg_device_info(int *sms, uint64_t *free_bytes, uint64_t *total_bytes) {
   size_t f = 0, t = 0;

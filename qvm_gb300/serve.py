@@ -210,15 +210,17 @@ class Server:
                 # (their tile passes run as short CTAs)
                 st.set_priority(1 if self.cost(req) <= self.fast_cost else -1)
                 prog = Program()
-                prog.add_gates(req.gates)
-                if req.fused:
-                    prog.plan(req.n, req.precision, fused=True, fusion_width=2)
-                prog.run(st, fused=req.fused)
-                draws = req.draws
-                if draws is None:
-                    draws = np.random.default_rng(0).random(req.shots)
-                shots = st.sample(draws)
-                prog.free()
+                try:  # the plan's device buffers are freed on every path
+                    prog.add_gates(req.gates)
+                    if req.fused:
+                        prog.plan(req.n, req.precision, fused=True, fusion_width=2)
+                    prog.run(st, fused=req.fused)
+                    draws = req.draws
+                    if draws is None:
+                        draws = np.random.default_rng(0).random(req.shots)
+                    shots = st.sample(draws)
+                finally:
+                    prog.free()
                 t1 = time.perf_counter()
                 fut.set_result(Result(shots, t0 - req.arrival, t1 - t0, t1 - req.arrival, req.tag))
             except Exception as e:  # the request fails, the server keeps going

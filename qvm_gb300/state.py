@@ -255,6 +255,9 @@ class Program:
 
     def __init__(self):
         self._h = ctypes.c_void_p()
+        # bumped by every added op: tuned choices cached for an older op list
+        # are not reused
+        self.generation = 0
         L.call("qvmg_program_create", ctypes.byref(self._h))
 
     def free(self):
@@ -270,15 +273,18 @@ class Program:
 
     def add_dense(self, matrix, qubits):
         m = _cplx(matrix)
+        self.generation += 1
         L.call("qvmg_program_add_dense", self._h, len(qubits), _qubit_array(qubits), _dptr(m))
 
     def add_permutation(self, perm, qubits):
         p = np.ascontiguousarray(perm, dtype=np.int64)
+        self.generation += 1
         L.call("qvmg_program_add_permutation", self._h, len(qubits), _qubit_array(qubits),
                p.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
 
     def add_diagonal(self, diag, qubits):
         d = _cplx(diag)
+        self.generation += 1
         L.call("qvmg_program_add_diagonal", self._h, len(qubits), _qubit_array(qubits), _dptr(d))
 
     def add_gates(self, gates):
@@ -291,6 +297,7 @@ class Program:
                              count=int(ks.sum()))
         mats = np.concatenate([np.asarray(m, dtype=np.complex128).ravel() for m, _ in gates])
         ip = ctypes.POINTER(ctypes.c_int)
+        self.generation += 1
         L.call("qvmg_program_add_dense_many", self._h, len(gates), ks.ctypes.data_as(ip),
                qubits.ctypes.data_as(ip), _dptr(mats))
         return self

@@ -1,4 +1,6 @@
 """GPU parity of the batched QAOA engine against the CPU oracle."""
+import os
+
 import numpy as np
 import pytest
 
@@ -78,3 +80,62 @@ def test_qaoa_batch_cut_paths(gpu, oracle):
         wex = float(np.sum(np.abs(want) ** 2 * circuits.maxcut_values(n, edges)))
         assert abs(ex[i] - wex) < 1e-5 * max(1.0, wex), (i, ex[i], wex)
     b.free()
+
+
+def test_qaoa_batch_full_size_instances_match_oracle(gpu, oracle):
+    """The workload's largest instances (n = 18, 20, 22) beside small ones,
+    against the oracle: amplitudes, <H_C> and 1024 shots per instance."""
+    oracle.set_workers(os.cpu_count() or 1)
+    graphs, gam, bet = random_qaoa_batch(5, [12, 18, 20, 22], 1, p=4, seed=9)
+    rng = np.random.default_rng(10)
+    big = [(n, circuits.random_3_regular_graph(n, rng)) for n in (18, 20, 22)]
+    graphs = big + graphs
+    gam = np.vstack([rng.uniform(0, np.pi, (3, 4)), gam])
+    bet = np.vstack([rng.uniform(0, np.pi / 2, (3, 4)), bet])
+    b = QaoaBatch(graphs, gam, bet)
+    draws = np.random.default_rng(11).random((len(graphs), 1024))
+    ex, shots = b.run(draws)
+    for i, (n, edges) in enumerate(graphs):
+        want = oracle_qaoa(oracle, n, edges, gam[i], bet[i])
+        got = b.state(i)
+        assert np.max(np.abs(got - want)) < 2e-6, (i, n)
+        wex = float(np.sum(np.abs(want) ** 2 * circuits.maxcut_values(n, edges)))
+        assert abs(ex[i] - wex) < 1e-5 * max(1.0, wex), (i, ex[i], wex)
+        ref = got.astype(np.complex64).astype(np.complex128)
+        tot = np.sum(np.abs(ref) ** 2)
+        wsh = oracle.sample_multiple(ref, draws[i] * tot)
+        cdf = np.cumsum(np.abs(ref) ** 2)
+        near = np.array([np.min(np.abs(cdf - d * tot)) < 1e-9 for d in draws[i]])
+        assert ((shots[i] == wsh) | near).all(), (i, n)
+    b.free()
+
+
+def test_qaoa_batch_shot_buffer_failure_leaves_batch_usable(gpu):
+    """Growing the shot buffers fails on its second allocation (made to fail
+    on the host through the library's test hook): the run reports
+    QVMG_E_NOMEM, and the batch then runs correctly with that shot count and
+    with the old one (no cached graph keeps the freed buffers)."""
+    from qvm_gb300 import QVMGError
+    from qvm_gb300 import _lib as L
+    graphs, gam, bet = random_qaoa_batch(3, [8, 12], 1, p=2, seed=7)
+    b = QaoaBatch(graphs, gam, bet)
+    rng = np.random.default_rng(3)
+    d4, d64 = rng.random((len(graphs), 4)), rng.random((len(graphs), 64))
+    e4, s4 = b.run(d4)
+    L.call("qvmg_debug_fail_alloc", 2)
+    try:
+        with pytest.raises(QVMGError, match="batch draws and shots") as err:
+            b.run(d64)
+        assert err.value.code == 3  # QVMG_E_NOMEM
+    finally:
+        L.call("qvmg_debug_fail_alloc", 0)
+    e4b, s4b = b.run(d4)
+    e64, s64 = b.run(d64)
+    fresh = QaoaBatch(graphs, gam, bet)
+    fe64, fs64 = fresh.run(d64)
+    np.testing.assert_array_equal(e4, e4b)
+    np.testing.assert_array_equal(s4, s4b)
+    np.testing.assert_array_equal(e64, fe64)
+    np.testing.assert_array_equal(s64, fs64)
+    b.free()
+    fresh.free()

@@ -5,6 +5,7 @@ import time
 from concurrent.futures import Future
 
 import numpy as np
+import pytest
 
 from qvm_gb300 import circuits
 from qvm_gb300.serve import Request, Server
@@ -132,3 +133,40 @@ def test_workers_lanes_eviction_and_priority(monkeypatch):
     # evicted states are freed outside the lock, so new states may briefly
     # overlap them: at most one evicted state per worker (5) beyond the budget
     assert _FakeState.peak <= budget + 5 * state_bytes(20, "fp64")
+
+
+def test_failed_request_frees_its_program(monkeypatch):
+    """A request whose run raises fails alone: its Program's device plan is
+    still freed, its state is released from the budget, and the server keeps
+    serving the next request."""
+    import threading
+    from qvm_gb300 import serve
+
+    class _Counting(_FakeProgram):
+        made = 0
+        freed = 0
+
+        def __init__(self):
+            _Counting.made += 1
+
+        def run(self, st, fused=True):
+            if self.ng == 13:
+                raise RuntimeError("planted run failure")
+
+        def free(self):
+            _Counting.freed += 1
+
+    monkeypatch.setattr(serve, "CudaPureState", _FakeState)
+    monkeypatch.setattr(serve, "Program", _Counting)
+    _FakeState.lock = threading.Lock()
+    _FakeState.live = _FakeState.peak = 0
+    srv = Server(hbm_budget=4 * state_bytes(14, "fp64"), workers=2, fast_workers=0,
+                 reserve_pool=False)
+    bad = srv.submit(Request(12, [None] * 13, 4, "fp64", np.zeros(4), True, "bad"))
+    good = srv.submit(Request(12, [None] * 5, 4, "fp64", np.zeros(4), True, "good"))
+    with pytest.raises(RuntimeError, match="planted"):
+        bad.result(timeout=30)
+    assert good.result(timeout=30).tag == "good"
+    srv.close()
+    assert _Counting.made == 2 and _Counting.freed == 2
+    assert _FakeState.live == 0

@@ -51,6 +51,39 @@ def test_noalloc_sampling_matches_allocating_sampler(gpu, prec):
     ref.free()
 
 
+def test_noalloc_at_its_30_qubit_limit(gpu):
+    """At 30 qubits the block sums fill the fixed array exactly (2^18 blocks
+    plus the total).  FP32 amplitudes made on the device, 300 draws of which
+    some sit at and near 1.0, on two calls in a row: identical to
+    qvmg_sample."""
+    import torch
+
+    n = 30
+    gen = torch.Generator(device="cuda").manual_seed(30)
+    amps = torch.randn(2 << n, dtype=torch.float32, device="cuda", generator=gen)
+    amps *= float(1.0 / torch.linalg.vector_norm(amps.double()).item())
+    ref = CudaPureState(n, "fp32")
+    ref.set_state_elements(amps.cpu().numpy().view(np.complex64).astype(np.complex128))
+    stream = torch.cuda.current_stream()
+    edge = np.array([0.0, 1e-12, 0.5, 1 - 2.0 ** -30, 1 - 1e-9, 1 - 1e-12, 1 - 2.0 ** -52, 1.0])
+    for call in range(2):
+        draws = np.concatenate([np.random.default_rng(300 + call).random(292), edge])
+        d_draws = torch.from_numpy(draws).cuda()
+        for rule, name in ((L.SAMPLE_BISECT, "bisect"), (L.SAMPLE_CDF, "cdf")):
+            d_out = torch.full((len(draws),), -1, dtype=torch.int64, device="cuda")
+            L.check(L.lib().qvmg_sample_noalloc(amps.data_ptr(), n, L.FP32,
+                                                d_draws.data_ptr(), len(draws), rule,
+                                                d_out.data_ptr(), stream.cuda_stream))
+            stream.synchronize()
+            got = d_out.cpu().numpy().astype(np.uint64)
+            want = ref.sample(draws, rule=name)
+            np.testing.assert_array_equal(got, want)
+            assert got[-1] < (1 << n)
+    ref.free()
+    del amps
+    torch.cuda.empty_cache()
+
+
 def test_noalloc_rejects_states_beyond_its_scratch(gpu):
     with pytest.raises(L.QVMGError, match="outside 1..30"):
         L.check(L.lib().qvmg_sample_noalloc(1, 31, L.FP32, 1, 1, L.SAMPLE_BISECT, 1, None))
