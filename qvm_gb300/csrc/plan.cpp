@@ -305,10 +305,14 @@ size_t tile_pass_smem_bytes(const Pass &p, int prec) {
   size_t b = ((size_t)1 << p.t) * csz + rows * 8;
   // (+ csz: a tensor-core operand starts on a 16-byte boundary)
   // (diagonal tables are read from global memory, not staged)
-  for (auto &o : p.tops)
+  bool tc = false;
+  for (auto &o : p.tops) {
     b += (o.kind == OP_DIAG ? 0 : o.data.size() * csz) + kTileOpDescBytes +
          (o.kind == OP_TC ? csz : 0);
+    tc = tc || o.kind == OP_TC;
+  }
   b += p.stages.size() * kTileStageDescBytes;
+  if (tc) b = ((b + 15) & ~(size_t)15) + kTcOperandSmemBytes;
   return (b + 15) & ~(size_t)15;
 }
 
@@ -431,20 +435,26 @@ static void plan_fused(const std::vector<Op> &ops, int nq, int prec, int fw, int
 
 // ---- tensor-core ops ---------------------------------------------------------------
 
-// TF32 rounding of an FP32 value: round to nearest, ties away from zero (the
-// device's cvt.rna.tf32.f32), kept as an FP32 value with 13 zero low bits.
-static float tf32_rna(float f) {
+// bf16 rounding of an FP32 value: round to nearest, ties to even (the
+// device's cvt.rn.bf16.f32), as its 16-bit pattern.
+static uint16_t bf16_rn(float f) {
   uint32_t u;
   std::memcpy(&u, &f, 4);
-  if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;
-  float r;
-  std::memcpy(&r, &u, 4);
-  return r;
+  if ((u & 0x7F800000u) == 0x7F800000u) return (uint16_t)(u >> 16);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
 }
 
-std::vector<float> tc_operand(const std::vector<cd> &m, int k) {
+static double bf16_value(uint16_t h) {
+  const uint32_t u = (uint32_t)h << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return (double)f;
+}
+
+std::vector<uint16_t> tc_operand(const std::vector<cd> &m, int k) {
   const int D = 1 << k, N = 2 * D, K = 2 * D;
-  std::vector<float> out((size_t)2 * N * K, 0.f);
+  std::vector<uint16_t> out((size_t)2 * N * K, 0);
   for (int n = 0; n < N; ++n)
     for (int kk = 0; kk < K; ++kk) {
       const int r = n >> 1, c = kk >> 1;
@@ -452,9 +462,9 @@ std::vector<float> tc_operand(const std::vector<cd> &m, int k) {
       double x;
       if ((n & 1) == 0) x = (kk & 1) == 0 ? z.real() : -z.imag();
       else x = (kk & 1) == 0 ? z.imag() : z.real();
-      const float hi = tf32_rna((float)x);
-      const float lo = tf32_rna((float)(x - (double)hi));
-      const size_t idx = (size_t)((n >> 3) * (K >> 2) + (kk >> 2)) * 32 + (n & 7) * 4 + (kk & 3);
+      const uint16_t hi = bf16_rn((float)x);
+      const uint16_t lo = bf16_rn((float)(x - bf16_value(hi)));
+      const size_t idx = (size_t)((n >> 3) * (K >> 3) + (kk >> 3)) * 64 + (n & 7) * 8 + (kk & 7);
       out[idx] = hi;
       out[(size_t)N * K + idx] = lo;
     }
@@ -520,10 +530,20 @@ void merge_tile_ops(Pass &p, int maxk, bool tensor_cores) {
     const int k = (int)op.pos.size();
     if (op.kind != OP_DENSE || k < kTcMinQubits || k > kTcMaxQubits) continue;
     if ((1 << (p.t - k)) < kTcRows) continue;  // fewer than 128 groups
-    const std::vector<float> f = tc_operand(op.data, k);
+    // The bf16 operand travels as the bit patterns of FP32 values (two bf16
+    // per float, the lower-addressed one in the low half): every such float
+    // is finite, so the FP32 upload of the pass data copies it unchanged.
+    const std::vector<uint16_t> h = tc_operand(op.data, k);
     op.kind = OP_TC;
-    op.data.resize(f.size() / 2);
-    for (size_t i = 0; i < op.data.size(); ++i) op.data[i] = cd(f[2 * i], f[2 * i + 1]);
+    op.data.resize(h.size() / 4);
+    for (size_t i = 0; i < op.data.size(); ++i) {
+      const uint32_t w0 = (uint32_t)h[4 * i] | ((uint32_t)h[4 * i + 1] << 16);
+      const uint32_t w1 = (uint32_t)h[4 * i + 2] | ((uint32_t)h[4 * i + 3] << 16);
+      float f0, f1;
+      std::memcpy(&f0, &w0, 4);
+      std::memcpy(&f1, &w1, 4);
+      op.data[i] = cd((double)f0, (double)f1);
+    }
   }
 }
 

@@ -12,10 +12,13 @@ using cd = std::complex<double>;
 enum OpKind { OP_DENSE = 0, OP_DIAG = 1, OP_PERM = 2, OP_TC = 3 };
 
 // Tensor-core tile ops: dense blocks of kTcMinQubits..kTcMaxQubits tile
-// bits run as tcgen05 TF32 MMAs over chunks of 128 groups.
+// bits run as tcgen05 bf16x3 MMAs over chunks of 128 groups.  A pass with
+// such ops also holds the MMA's A operand buffers in shared memory (two
+// chunks of 4-qubit groups, 16 KiB each, plus 128-byte alignment).
 constexpr int kTcMinQubits = 3;
 constexpr int kTcMaxQubits = 4;
 constexpr int kTcRows = 128;
+constexpr size_t kTcOperandSmemBytes = 2 * 16384 + 128;
 
 // One gate application (or fused block).  Qubits are in nat-tuple order:
 // q[j] is bit j of the matrix index.
@@ -89,10 +92,10 @@ struct Plan {
 
 // Tensor-core operand of a dense k-qubit block (k = 3, 4): the real form
 // Bt[n][kk] (n = 2r + re/im of output r, kk = 2c + re/im of input c), split
-// into TF32 hi and lo parts (round to nearest, ties away), each laid out
-// K-major in 8x4 core matrices: element (n, kk) at float
-// ((n/8)*(2D/4) + kk/4)*32 + (n%8)*4 + kk%4; hi block, then lo block.
-std::vector<float> tc_operand(const std::vector<cd> &m, int k);
+// into bf16 hi and lo parts (round to nearest even; lo = bf16(x - hi)),
+// each laid out K-major in 8-row x 8-element core matrices: element (n, kk)
+// at ((n/8)*(2D/8) + kk/8)*64 + (n%8)*8 + kk%8; hi block, then lo block.
+std::vector<uint16_t> tc_operand(const std::vector<cd> &m, int k);
 // Merge a tile pass's dense ops into blocks of at most `maxk` tile bits
 // (moving an op past ops on disjoint qubits), then turn the blocks that fit
 // the tensor-core path into OP_TC ops.

@@ -26,6 +26,7 @@
 // This is the GB300 form of the reference's per-gate complement iteration
 // (src/wavefunction.lisp:155-306, src/compile-gate.lisp:23-209): the same
 // gather -> matvec -> scatter, for many gates per HBM round trip.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -432,26 +433,31 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
   for (int r = 0; r < (1 << R); ++r) tile[lo[r & 3] ^ hi[r >> 2]] = v[r];
 }
 
-// ---- tensor-core ops (FP32, tcgen05) ---------------------------------------------------
+// ---- tensor-core ops (FP32 state, tcgen05, BF16x3) ----------------------------------
 //
 // A dense block on k = 3 or 4 tile bits is a real GEMM per chunk of 128
 // groups: D[g][n] = sum_kk A[g][kk] Bt[n][kk], with A[g] the group's 2^k
 // amplitudes as (re, im) pairs and Bt the block's real form (n = 2r + re/im
-// of output r).  Operands are split into TF32 hi + lo parts and
-// D = Ahi*Bhi + (Ahi*Blo + Alo*Bhi) is accumulated in FP32 in tensor memory,
-// the large product and the two small ones in separate columns that are
-// added on read-out.  A is written to tensor memory by the threads
-// (row g = TMEM lane g, one thread per row and half-row: warps w and w+4
-// share the lanes of sub-partition w%4 and take the two halves of the
-// group), Bt comes from the pass data in shared memory (split on the host,
-// K-major 8x4 core matrices).  A ninth warp issues the MMAs and commits
-// them to an mbarrier that the eight data warps wait on with a bounded loop.
+// of output r).  Both operands are split into bf16 hi + lo parts and the
+// three products that carry 16 significant bits are accumulated in FP32 in
+// one tensor-memory accumulator:
+//     D = Ahi*Bhi + Alo*Bhi + Ahi*Blo
+// (the bf16x3 scheme; the dropped Alo*Blo term and the parts' own rounding
+// are ~2^-17 relative).  The data warps write A into shared memory in the
+// canonical K-major layout -- row g = group g, [hi reals | lo reals], 8-row x
+// 16-byte core matrices -- and the MMA reads it through a descriptor; Bt
+// (split on the host) sits in the pass data in the same layout, hi then lo.
+// Eight data warps serve a chunk, two threads per group (warps w and w+4
+// take the two halves of a group's amplitudes and read back the matching
+// halves of D from TMEM sub-partition w%4); a ninth warp issues the MMAs,
+// 3 per 16-element K step, and commits them to an mbarrier that the data
+// warps wait on with a bounded loop.
 //
-// Chunks are software-pipelined over two TMEM buffer sets (each: D | A hi |
-// A lo) and two barriers: while the MMAs of chunk c are issued and run, the
-// data warps read out and scatter chunk c-1 and gather chunk c+1.
-constexpr int kTcCols = 256;           // TMEM columns per CTA: 2 buffers x 128
-constexpr int kTcBufCols = 128;
+// Chunks are software-pipelined over two A buffers, two D buffers and two
+// barriers: while the MMAs of chunk c run, the data warps read out and
+// scatter chunk c-1 and gather chunk c+1.
+constexpr int kTcCols = 64;            // TMEM columns per CTA: 2 D buffers of 32
+constexpr int kTcBufCols = 32;
 constexpr int kTcWaitLimit = 1 << 22;  // polls of an MMA barrier before giving up
 
 struct TcCtx {
@@ -459,50 +465,28 @@ struct TcCtx {
   uint32_t mbar[2];   // shared addresses of the two MMA-completion barriers
   uint32_t phase[2];  // parity of the phase each barrier's next wait is for
   int ok;             // 0 once a wait gave up
+  uint32_t abuf;      // shared address of the two A operand buffers
+  unsigned char *abuf_p;  // the same, as a generic pointer
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ uint32_t tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return r;
-}
-
-// Shared-memory matrix descriptor: K-major, no swizzle; the next 4-element
+// Shared-memory matrix descriptor: K-major, no swizzle; the next 16-byte
 // core matrix along K is 128 bytes on, the next 8 rows `sbo` bytes on.
 __device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t sbo) {
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) |
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-__device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t idesc,
+// D[tmem] (+)= A[smem] * B[smem]^T, bf16 operands, FP32 accumulation.
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                        uint32_t accumulate) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
-      "r"(a), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-template <int NR>
-__device__ __forceinline__ void tmem_st(uint32_t taddr, const uint32_t (&r)[NR]);
-template <>
-__device__ __forceinline__ void tmem_st<8>(uint32_t taddr, const uint32_t (&r)[8]) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"r"(
-                   taddr),
-               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
-               "r"(r[7]));
-}
-template <>
-__device__ __forceinline__ void tmem_st<16>(uint32_t taddr, const uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
-      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
-      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
-      "r"(r[15]));
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 template <int NR>
@@ -538,10 +522,35 @@ __device__ __forceinline__ uint32_t tc_wait(uint32_t mbar, uint32_t phase) {
   return done;
 }
 
+// bf16 hi/lo split of an amplitude (re, im): hi = bf16(x) (round to nearest
+// even), lo = bf16(x - hi); each pair packed with re in the low half.
+__device__ __forceinline__ void bf16_split(float2 v, uint32_t &hi, uint32_t &lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
+  hi = *reinterpret_cast<const uint32_t *>(&h);
+  lo = *reinterpret_cast<const uint32_t *>(&l);
+}
+
+// The two A operand buffers of a tensor-core pass follow the stage
+// descriptors in dynamic shared memory, 128-byte aligned.
+__device__ __forceinline__ unsigned char *tc_abuf(TileStageDev *stages, int nstages) {
+  const uintptr_t e = reinterpret_cast<uintptr_t>(stages + nstages);
+  return reinterpret_cast<unsigned char *>((e + 127) & ~(uintptr_t)127);
+}
+
 template <int K>
-__device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op, const float *bmat,
-                                        TcCtx &ctx, volatile int *abort_flag) {
+__device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op,
+                                        const unsigned char *bmat, TcCtx &ctx,
+                                        volatile int *abort_flag) {
   constexpr int D = 1 << K, NC = 2 * D, H = D / 2;
+  constexpr uint32_t kRowBytes = 8 * D;       // A row: 2D hi + 2D lo bf16
+  constexpr uint32_t kSboA = 8 * kRowBytes;   // 8 rows of (kRowBytes / 16) core matrices
+  constexpr uint32_t kSboB = 2 * 16 * D;      // B rows have 2D bf16 = 4D bytes; 8 rows per group
+  constexpr uint32_t kPieceB = 8 * D * D;     // bytes of Bt hi (then Bt lo)
+  constexpr uint32_t kABuf = kTcABufBytes;  // buffer stride (sized for K = 4)
+  static_assert(kTileTcRows * kRowBytes <= kTcABufBytes, "A operand buffer");
+  constexpr int kSteps = NC / 16;             // 16-element K steps per piece
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool issuer = warp == kTileThreads / 32;  // the extra warp issues the MMAs
   const int sub = warp & 3, half = (warp >> 2) & 1;
@@ -567,44 +576,42 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
       if ((c >> j) & 1) o |= 1u << op.pos[j];
     off[i] = o;
   }
-  // Per buffer: columns [0, NC) = Ahi*Bhi, [NC, 2NC) = Ahi*Blo + Alo*Bhi,
-  // then A hi and A lo.  The operand's hi and lo blocks are consecutive
-  // 8-row groups, i.e. one K-major matrix [Bhi | Blo] of 2*NC rows, so
-  // Ahi*[Bhi | Blo] is a single MMA of N = 2*NC.
-  const uint32_t idesc_w = (1u << 4) | (2u << 7) | (2u << 10) |
-                           ((uint32_t)((2 * NC) >> 3) << 17) |
-                           ((uint32_t)(kTileTcRows >> 4) << 24);
-  const uint32_t idesc_n = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NC >> 3) << 17) |
-                           ((uint32_t)(kTileTcRows >> 4) << 24);
-  const uint32_t col_ahi = 2 * NC, col_alo = 3 * NC;
+  // instruction descriptor: D f32, A and B bf16, both K-major, N = NC, M = 128
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NC >> 3) << 17) |
+                         ((uint32_t)(kTileTcRows >> 4) << 24);
   const uint32_t lanes = (uint32_t)(sub * 32) << 16;
   const uint32_t bhi = smem_u32(bmat);
-  const uint32_t sbo = (NC / 4) * 128;
   const unsigned nchunks = (1u << (t - K)) / kTileTcRows;
+  const unsigned row = sub * 32 + lane;  // this thread's A row (group within a chunk)
+  const uint32_t arow = (row >> 3) * kSboA + (row & 7) * 16;
   auto group_base = [&](unsigned ch) {
-    unsigned b = ch * kTileTcRows + sub * 32 + lane;
+    unsigned b = ch * kTileTcRows + row;
 #pragma unroll
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
     return b;
   };
   for (unsigned ch = 0; ch <= nchunks; ++ch) {
-    const uint32_t buf = ctx.tmem + (ch & 1u) * kTcBufCols;
+    const uint32_t abuf = ctx.abuf + (ch & 1u) * kABuf;
+    unsigned char *abuf_p = ctx.abuf_p + (ch & 1u) * kABuf;
     if (!issuer && ch < nchunks) {
-      // gather + split chunk ch into this buffer's A columns (its previous
-      // MMAs, chunk ch-2, completed and were read out last iteration)
+      // gather + split chunk ch into this buffer (its previous MMAs, chunk
+      // ch-2, completed and were read out last iteration)
       const unsigned b = group_base(ch);
-      uint32_t hi[D], lo[D];
+      uint32_t hi[H], lo[H];
 #pragma unroll
-      for (int i = 0; i < H; ++i) {
-        const float2 v = tile[b | off[i]];
-        hi[2 * i] = tf32_rna(v.x);
-        lo[2 * i] = tf32_rna(v.x - __uint_as_float(hi[2 * i]));
-        hi[2 * i + 1] = tf32_rna(v.y);
-        lo[2 * i + 1] = tf32_rna(v.y - __uint_as_float(hi[2 * i + 1]));
+      for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
+      unsigned char *arow_p = abuf_p + arow;
+#pragma unroll
+      for (int j = 0; j < H / 4; ++j) {
+        // 4 amplitudes = 8 bf16 = one 16-byte core-matrix row; hi k-group
+        // half*H/4 + j, lo k-group D/4 + half*H/4 + j
+        *reinterpret_cast<uint4 *>(arow_p + (half * (H / 4) + j) * 128) =
+            make_uint4(hi[4 * j], hi[4 * j + 1], hi[4 * j + 2], hi[4 * j + 3]);
+        *reinterpret_cast<uint4 *>(arow_p + (D / 4 + half * (H / 4) + j) * 128) =
+            make_uint4(lo[4 * j], lo[4 * j + 1], lo[4 * j + 2], lo[4 * j + 3]);
       }
-      tmem_st<D>(buf + lanes + col_ahi + half * D, hi);
-      tmem_st<D>(buf + lanes + col_alo + half * D, lo);
-      asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+      // the tensor core reads A through the async proxy
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -615,11 +622,18 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     }
     if (issuer) {
       if (ch < nchunks && lane == 0) {
+        const uint32_t dcol = ctx.tmem + (ch & 1u) * kTcBufCols;
 #pragma unroll
-        for (int s = 0; s < NC / 8; ++s) {
-          tc_mma(buf, buf + col_ahi + 8 * s, tc_desc(bhi + s * 256, sbo), idesc_w, s > 0);
-          tc_mma(buf + NC, buf + col_alo + 8 * s, tc_desc(bhi + s * 256, sbo), idesc_n, 1);
-        }
+        for (int s = 0; s < kSteps; ++s)  // Ahi * Bhi
+          tc_mma(dcol, tc_desc(abuf + s * 256, kSboA), tc_desc(bhi + s * 256, kSboB), idesc, s > 0);
+#pragma unroll
+        for (int s = 0; s < kSteps; ++s)  // + Alo * Bhi
+          tc_mma(dcol, tc_desc(abuf + (D / 4) * 128 + s * 256, kSboA),
+                 tc_desc(bhi + s * 256, kSboB), idesc, 1);
+#pragma unroll
+        for (int s = 0; s < kSteps; ++s)  // + Ahi * Blo
+          tc_mma(dcol, tc_desc(abuf + s * 256, kSboA), tc_desc(bhi + kPieceB + s * 256, kSboB),
+                 idesc, 1);
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 ctx.mbar[ch & 1u])
@@ -634,17 +648,13 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
       }
       ctx.phase[pb] ^= 1u;
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t pbuf = ctx.tmem + pb * kTcBufCols + lanes;
-      uint32_t r0[D], r1[D];
-      tmem_ld<D>(pbuf + half * D, r0);
-      tmem_ld<D>(pbuf + NC + half * D, r1);
+      uint32_t r[D];
+      tmem_ld<D>(ctx.tmem + pb * kTcBufCols + lanes + half * D, r);
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
       const unsigned b = group_base(ch - 1);
 #pragma unroll
       for (int i = 0; i < H; ++i)
-        tile[b | off[i]] =
-            make_float2(__uint_as_float(r0[2 * i]) + __uint_as_float(r1[2 * i]),
-                        __uint_as_float(r0[2 * i + 1]) + __uint_as_float(r1[2 * i + 1]));
+        tile[b | off[i]] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
     }
   }
   __syncthreads();  // a wait that gave up on the last chunk is seen here
@@ -808,7 +818,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   __shared__ __align__(8) unsigned long long tc_mbar[2];
   __shared__ uint32_t tc_tmem_slot;
   __shared__ int tc_abort;
-  TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1};
+  TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1, 0u, nullptr};
   if constexpr (RB < 0) {
     if ((threadIdx.x >> 5) == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -856,6 +866,8 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     ctx.tmem = tc_tmem_slot;
+    ctx.abuf_p = tc_abuf(stages, p.nstages);
+    ctx.abuf = smem_u32(ctx.abuf_p);
     ctx.mbar[0] = smem_u32(&tc_mbar[0]);
     ctx.mbar[1] = smem_u32(&tc_mbar[1]);
   }
@@ -904,7 +916,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
       const TileOpDev &op = ops[st.first];
       if constexpr (RB < 0) {
         if (op.kind == 3) {
-          const float *bm = reinterpret_cast<const float *>(data + op.data);
+          const unsigned char *bm = reinterpret_cast<const unsigned char *>(data + op.data);
           if (op.k == 3) tile_tc<3>(reinterpret_cast<float2 *>(tile), t, op, bm, ctx, &tc_abort);
           else tile_tc<4>(reinterpret_cast<float2 *>(tile), t, op, bm, ctx, &tc_abort);
           if (!ctx.ok) break;
@@ -945,12 +957,13 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   }
 }
 
-size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages) {
+size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages, int tc) {
   size_t csz = prec == QVMG_FP64 ? 16 : 8;
   size_t rows = ((size_t)1 << (t - L)) + 1 & ~(size_t)1;  // padded to 16 bytes
   size_t b = ((size_t)1 << t) * csz + rows * 8 + (size_t)ndata * csz +
              (size_t)nops * sizeof(TileOpDev) + (size_t)nstages * sizeof(TileStageDev);
-  return (b + 15) & ~(size_t)15;
+  b = (b + 15) & ~(size_t)15;
+  return tc ? b + kTcAOperandBytes : b;
 }
 
 template <typename T, int KMAX, int RB>
@@ -1016,7 +1029,8 @@ static int tile_launch_r(qvmg_state s, const TileArgs &args, size_t smem) {
 }
 
 int launch_tile(qvmg_state s, const TileArgs &args) {
-  size_t smem = tile_smem_bytes(s->prec, args.t, args.L, args.ndata, args.nops, args.nstages);
+  size_t smem = tile_smem_bytes(s->prec, args.t, args.L, args.ndata, args.nops, args.nstages,
+                               args.tc);
   if (smem > (size_t)kTileMaxSmem) return fail(QVMG_E_UNSUPPORTED, "tile pass exceeds shared memory");
   if (args.kmax < 1 || args.kmax > 5) return fail(QVMG_E_INVALID, "tile op width out of range");
   if (s->prec == QVMG_FP64) {

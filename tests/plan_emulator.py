@@ -20,16 +20,22 @@ def _apply_table(wf, qubits, table):
 
 
 def tc_matrix(pairs, k):
-    """The complex block of a tensor-core tile op from its operand: the TF32
+    """The complex block of a tensor-core tile op from its operand: the bf16
     hi + lo parts of the real form Bt (n = 2r + re/im of output r,
-    kk = 2c + re/im of input c), K-major 8x4 core matrices."""
-    f = np.array(pairs, dtype=np.float64).reshape(-1)
+    kk = 2c + re/im of input c), K-major 8x8 core matrices, carried as the
+    bit patterns of FP32 values (two bf16 per float, low half first)."""
+    f = np.array(pairs, dtype=np.float64).reshape(-1).astype(np.float32)
+    h = f.view(np.uint32)
+    u16 = np.empty(2 * len(h), dtype=np.uint32)
+    u16[0::2] = h & 0xFFFF
+    u16[1::2] = h >> 16
+    vals = (u16 << 16).astype(np.uint32).view(np.float32).astype(np.float64)
     d = 1 << k
     nk = 2 * d
     n = np.arange(nk)[:, None]
     kk = np.arange(nk)[None, :]
-    idx = ((n >> 3) * (nk >> 2) + (kk >> 2)) * 32 + (n & 7) * 4 + (kk & 3)
-    bt = f[idx] + f[nk * nk + idx]
+    idx = ((n >> 3) * (nk >> 3) + (kk >> 3)) * 64 + (n & 7) * 8 + (kk & 7)
+    bt = vals[idx] + vals[nk * nk + idx]
     re, im = bt[0::2, 0::2], bt[1::2, 0::2]
     assert np.array_equal(bt[1::2, 1::2], re) and np.array_equal(bt[0::2, 1::2], -im)
     return re + 1j * im

@@ -98,8 +98,9 @@ def test_fused_plan_equals_circuit(oracle, prec, fw, tile):
 @pytest.mark.parametrize("fw,tile", [(2, 0), (4, 0), (2, 11), (4, 12), (1, 13)])
 def test_tensor_core_plan_equals_circuit(oracle, fw, tile):
     """FP32 tensor-core planning: the pass-local merge into blocks of <= 4
-    tile bits and the split TF32 operand, executed on the oracle, equal the
-    unfused circuit to the hi + lo precision (~2^-22 relative per block)."""
+    tile bits and the split bf16 operand, executed on the oracle, equal the
+    unfused circuit to the hi + lo precision of the block (~2^-17 relative
+    per entry)."""
     n = 16
     for name, gs in [("su", circuits.random_su_circuit(n, depth=5, seed=fw + tile)),
                      ("layers", circuits.random_layers(n, layers=3, seed=6)),
