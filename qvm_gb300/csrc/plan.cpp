@@ -305,14 +305,10 @@ size_t tile_pass_smem_bytes(const Pass &p, int prec) {
   size_t b = ((size_t)1 << p.t) * csz + rows * 8;
   // (+ csz: a tensor-core operand starts on a 16-byte boundary)
   // (diagonal tables are read from global memory, not staged)
-  bool tc = false;
-  for (auto &o : p.tops) {
+  for (auto &o : p.tops)
     b += (o.kind == OP_DIAG ? 0 : o.data.size() * csz) + kTileOpDescBytes +
          (o.kind == OP_TC ? csz : 0);
-    tc = tc || o.kind == OP_TC;
-  }
   b += p.stages.size() * kTileStageDescBytes;
-  if (tc) b = ((b + 15) & ~(size_t)15) + kTcOperandSmemBytes;
   return (b + 15) & ~(size_t)15;
 }
 

@@ -12,13 +12,10 @@ using cd = std::complex<double>;
 enum OpKind { OP_DENSE = 0, OP_DIAG = 1, OP_PERM = 2, OP_TC = 3 };
 
 // Tensor-core tile ops: dense blocks of kTcMinQubits..kTcMaxQubits tile
-// bits run as tcgen05 bf16x3 MMAs over chunks of 128 groups.  A pass with
-// such ops also holds the MMA's A operand buffers in shared memory (two
-// chunks of 4-qubit groups, 16 KiB each, plus 128-byte alignment).
+// bits run as tcgen05 bf16x3 MMAs over chunks of 128 groups.
 constexpr int kTcMinQubits = 3;
 constexpr int kTcMaxQubits = 4;
 constexpr int kTcRows = 128;
-constexpr size_t kTcOperandSmemBytes = 2 * 16384 + 128;
 
 // One gate application (or fused block).  Qubits are in nat-tuple order:
 // q[j] is bit j of the matrix index.

@@ -29,7 +29,6 @@ static_assert(sizeof(TileOpDev) == kTileOpDescBytes, "planner op descriptor size
 static_assert(sizeof(TileStageDev) == kTileStageDescBytes, "planner stage descriptor size");
 static_assert(kTileMaxSmem == (int)kTileSmemBudget, "planner shared-memory budget");
 static_assert(kTileTcRows == kTcRows, "tensor-core chunk rows");
-static_assert(kTcAOperandBytes == kTcOperandSmemBytes, "tensor-core operand buffers");
 
 // Device image of one plan for one precision.
 struct DevicePlan {
@@ -295,8 +294,7 @@ static int build_device_plan(qvmg_program p, int nq, int prec, int mode, int fw,
       ta.ops = (const void *)ops_off;
       ta.stages = (const void *)stages_off;
       ta.tables = (const void *)tables_off;
-      if (tile_smem_bytes(prec, ta.t, ta.L, ta.ndata, ta.nops, ta.nstages, ta.tc) >
-          (size_t)kTileMaxSmem)
+      if (tile_smem_bytes(prec, ta.t, ta.L, ta.ndata, ta.nops, ta.nstages) > (size_t)kTileMaxSmem)
         return fail(QVMG_E_UNSUPPORTED, "tile pass data exceeds shared memory");
     }
   }

@@ -443,21 +443,23 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 // one tensor-memory accumulator:
 //     D = Ahi*Bhi + Alo*Bhi + Ahi*Blo
 // (the bf16x3 scheme; the dropped Alo*Blo term and the parts' own rounding
-// are ~2^-17 relative).  The data warps write A into shared memory in the
-// canonical K-major layout -- row g = group g, [hi reals | lo reals], 8-row x
-// 16-byte core matrices -- and the MMA reads it through a descriptor; Bt
-// (split on the host) sits in the pass data in the same layout, hi then lo.
-// Eight data warps serve a chunk, two threads per group (warps w and w+4
-// take the two halves of a group's amplitudes and read back the matching
-// halves of D from TMEM sub-partition w%4); a ninth warp issues the MMAs,
-// 3 per 16-element K step, and commits them to an mbarrier that the data
-// warps wait on with a bounded loop.
+// are ~2^-17 relative).  A lives in tensor memory, written by the threads
+// with tcgen05.st: TMEM lane g = group g, bf16 pairs packed two to a 32-bit
+// column, the hi part in columns [0, D) and the lo part in [D, 2D).  Bt
+// (split on the host) sits in the pass data in shared memory, K-major in
+// 8-row x 16-byte core matrices, hi then lo.  Eight data warps serve a
+// chunk, two threads per group: warps w and w+4 take the two halves of a
+// group's amplitudes and write and read the matching columns of TMEM
+// sub-partition w%4.  A ninth warp issues the MMAs, 3 per 16-element K step,
+// and commits them to an mbarrier that the data warps wait on with a
+// bounded loop.
 //
-// Chunks are software-pipelined over two A buffers, two D buffers and two
+// Chunks are software-pipelined over two TMEM buffers (each D | A) and two
 // barriers: while the MMAs of chunk c run, the data warps read out and
 // scatter chunk c-1 and gather chunk c+1.
-constexpr int kTcCols = 64;            // TMEM columns per CTA: 2 D buffers of 32
-constexpr int kTcBufCols = 32;
+constexpr int kTcCols = 128;           // TMEM columns per CTA: 2 buffers of 64
+constexpr int kTcBufCols = 64;         // D in [0, 32), A in [32, 64)
+constexpr int kTcACol = 32;
 constexpr int kTcWaitLimit = 1 << 22;  // polls of an MMA barrier before giving up
 
 struct TcCtx {
@@ -465,8 +467,6 @@ struct TcCtx {
   uint32_t mbar[2];   // shared addresses of the two MMA-completion barriers
   uint32_t phase[2];  // parity of the phase each barrier's next wait is for
   int ok;             // 0 once a wait gave up
-  uint32_t abuf;      // shared address of the two A operand buffers
-  unsigned char *abuf_p;  // the same, as a generic pointer
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -480,13 +480,31 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t sbo) {
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-// D[tmem] (+)= A[smem] * B[smem]^T, bf16 operands, FP32 accumulation.
-__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+// D[tmem] (+)= A[tmem] * B[smem]^T, bf16 operands, FP32 accumulation.
+__device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t idesc,
                                        uint32_t accumulate) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+      "r"(a), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+template <int NR>
+__device__ __forceinline__ void tmem_st(uint32_t taddr, const uint32_t (&r)[NR]);
+template <>
+__device__ __forceinline__ void tmem_st<4>(uint32_t taddr, const uint32_t (&r)[4]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};\n" ::"r"(taddr),
+               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3])
+               : "memory");
+}
+template <>
+__device__ __forceinline__ void tmem_st<8>(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"r"(
+                   taddr),
+               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+               "r"(r[7])
+               : "memory");
 }
 
 template <int NR>
@@ -532,25 +550,15 @@ __device__ __forceinline__ void bf16_split(float2 v, uint32_t &hi, uint32_t &lo)
   lo = *reinterpret_cast<const uint32_t *>(&l);
 }
 
-// The two A operand buffers of a tensor-core pass follow the stage
-// descriptors in dynamic shared memory, 128-byte aligned.
-__device__ __forceinline__ unsigned char *tc_abuf(TileStageDev *stages, int nstages) {
-  const uintptr_t e = reinterpret_cast<uintptr_t>(stages + nstages);
-  return reinterpret_cast<unsigned char *>((e + 127) & ~(uintptr_t)127);
-}
-
 template <int K>
 __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op,
                                         const unsigned char *bmat, TcCtx &ctx,
                                         volatile int *abort_flag) {
   constexpr int D = 1 << K, NC = 2 * D, H = D / 2;
-  constexpr uint32_t kRowBytes = 8 * D;       // A row: 2D hi + 2D lo bf16
-  constexpr uint32_t kSboA = 8 * kRowBytes;   // 8 rows of (kRowBytes / 16) core matrices
-  constexpr uint32_t kSboB = 2 * 16 * D;      // B rows have 2D bf16 = 4D bytes; 8 rows per group
-  constexpr uint32_t kPieceB = 8 * D * D;     // bytes of Bt hi (then Bt lo)
-  constexpr uint32_t kABuf = kTcABufBytes;  // buffer stride (sized for K = 4)
-  static_assert(kTileTcRows * kRowBytes <= kTcABufBytes, "A operand buffer");
-  constexpr int kSteps = NC / 16;             // 16-element K steps per piece
+  constexpr uint32_t kSboB = 2 * 16 * D;   // Bt rows hold 2D bf16 (4D bytes); 8 rows per group
+  constexpr uint32_t kPieceB = 8 * D * D;  // bytes of Bt hi (then Bt lo)
+  constexpr int kSteps = NC / 16;          // 16-element K steps per piece (8 TMEM columns)
+  static_assert(NC <= kTcACol && 2 * D <= kTcBufCols - kTcACol, "TMEM buffer layout");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool issuer = warp == kTileThreads / 32;  // the extra warp issues the MMAs
   const int sub = warp & 3, half = (warp >> 2) & 1;
@@ -582,36 +590,24 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
   const uint32_t lanes = (uint32_t)(sub * 32) << 16;
   const uint32_t bhi = smem_u32(bmat);
   const unsigned nchunks = (1u << (t - K)) / kTileTcRows;
-  const unsigned row = sub * 32 + lane;  // this thread's A row (group within a chunk)
-  const uint32_t arow = (row >> 3) * kSboA + (row & 7) * 16;
   auto group_base = [&](unsigned ch) {
-    unsigned b = ch * kTileTcRows + row;
+    unsigned b = ch * kTileTcRows + sub * 32 + lane;
 #pragma unroll
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
     return b;
   };
   for (unsigned ch = 0; ch <= nchunks; ++ch) {
-    const uint32_t abuf = ctx.abuf + (ch & 1u) * kABuf;
-    unsigned char *abuf_p = ctx.abuf_p + (ch & 1u) * kABuf;
+    const uint32_t buf = ctx.tmem + (ch & 1u) * kTcBufCols;
     if (!issuer && ch < nchunks) {
-      // gather + split chunk ch into this buffer (its previous MMAs, chunk
-      // ch-2, completed and were read out last iteration)
+      // gather + split chunk ch into this buffer's A columns (its previous
+      // MMAs, chunk ch-2, completed and were read out last iteration)
       const unsigned b = group_base(ch);
       uint32_t hi[H], lo[H];
 #pragma unroll
       for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
-      unsigned char *arow_p = abuf_p + arow;
-#pragma unroll
-      for (int j = 0; j < H / 4; ++j) {
-        // 4 amplitudes = 8 bf16 = one 16-byte core-matrix row; hi k-group
-        // half*H/4 + j, lo k-group D/4 + half*H/4 + j
-        *reinterpret_cast<uint4 *>(arow_p + (half * (H / 4) + j) * 128) =
-            make_uint4(hi[4 * j], hi[4 * j + 1], hi[4 * j + 2], hi[4 * j + 3]);
-        *reinterpret_cast<uint4 *>(arow_p + (D / 4 + half * (H / 4) + j) * 128) =
-            make_uint4(lo[4 * j], lo[4 * j + 1], lo[4 * j + 2], lo[4 * j + 3]);
-      }
-      // the tensor core reads A through the async proxy
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      tmem_st<H>(buf + lanes + kTcACol + half * H, hi);
+      tmem_st<H>(buf + lanes + kTcACol + D + half * H, lo);
+      asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -622,18 +618,16 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     }
     if (issuer) {
       if (ch < nchunks && lane == 0) {
-        const uint32_t dcol = ctx.tmem + (ch & 1u) * kTcBufCols;
+        const uint32_t a = buf + kTcACol;
 #pragma unroll
         for (int s = 0; s < kSteps; ++s)  // Ahi * Bhi
-          tc_mma(dcol, tc_desc(abuf + s * 256, kSboA), tc_desc(bhi + s * 256, kSboB), idesc, s > 0);
+          tc_mma(buf, a + 8 * s, tc_desc(bhi + s * 256, kSboB), idesc, s > 0);
 #pragma unroll
         for (int s = 0; s < kSteps; ++s)  // + Alo * Bhi
-          tc_mma(dcol, tc_desc(abuf + (D / 4) * 128 + s * 256, kSboA),
-                 tc_desc(bhi + s * 256, kSboB), idesc, 1);
+          tc_mma(buf, a + D + 8 * s, tc_desc(bhi + s * 256, kSboB), idesc, 1);
 #pragma unroll
         for (int s = 0; s < kSteps; ++s)  // + Ahi * Blo
-          tc_mma(dcol, tc_desc(abuf + s * 256, kSboA), tc_desc(bhi + kPieceB + s * 256, kSboB),
-                 idesc, 1);
+          tc_mma(buf, a + 8 * s, tc_desc(bhi + kPieceB + s * 256, kSboB), idesc, 1);
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 ctx.mbar[ch & 1u])
@@ -818,7 +812,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   __shared__ __align__(8) unsigned long long tc_mbar[2];
   __shared__ uint32_t tc_tmem_slot;
   __shared__ int tc_abort;
-  TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1, 0u, nullptr};
+  TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1};
   if constexpr (RB < 0) {
     if ((threadIdx.x >> 5) == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -866,8 +860,6 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     ctx.tmem = tc_tmem_slot;
-    ctx.abuf_p = tc_abuf(stages, p.nstages);
-    ctx.abuf = smem_u32(ctx.abuf_p);
     ctx.mbar[0] = smem_u32(&tc_mbar[0]);
     ctx.mbar[1] = smem_u32(&tc_mbar[1]);
   }
@@ -957,13 +949,12 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   }
 }
 
-size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages, int tc) {
+size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages) {
   size_t csz = prec == QVMG_FP64 ? 16 : 8;
   size_t rows = ((size_t)1 << (t - L)) + 1 & ~(size_t)1;  // padded to 16 bytes
   size_t b = ((size_t)1 << t) * csz + rows * 8 + (size_t)ndata * csz +
              (size_t)nops * sizeof(TileOpDev) + (size_t)nstages * sizeof(TileStageDev);
-  b = (b + 15) & ~(size_t)15;
-  return tc ? b + kTcAOperandBytes : b;
+  return (b + 15) & ~(size_t)15;
 }
 
 template <typename T, int KMAX, int RB>
@@ -1029,8 +1020,7 @@ static int tile_launch_r(qvmg_state s, const TileArgs &args, size_t smem) {
 }
 
 int launch_tile(qvmg_state s, const TileArgs &args) {
-  size_t smem = tile_smem_bytes(s->prec, args.t, args.L, args.ndata, args.nops, args.nstages,
-                               args.tc);
+  size_t smem = tile_smem_bytes(s->prec, args.t, args.L, args.ndata, args.nops, args.nstages);
   if (smem > (size_t)kTileMaxSmem) return fail(QVMG_E_UNSUPPORTED, "tile pass exceeds shared memory");
   if (args.kmax < 1 || args.kmax > 5) return fail(QVMG_E_INVALID, "tile op width out of range");
   if (s->prec == QVMG_FP64) {

@@ -20,10 +20,6 @@ constexpr int kTileThreadsSmem = 128;
 constexpr int kTileMaxSmem = 227 * 1024 - 64;
 constexpr int kTileMaxE = 24;
 constexpr int kTileTcRows = 128;  // groups per tensor-core chunk (MMA M)
-// Shared memory of the tensor-core A operand: two chunk buffers of 128
-// groups x 4-qubit rows (64 bf16 = 128 bytes), after 128-byte alignment.
-constexpr int kTcABufBytes = kTileTcRows * 128;
-constexpr size_t kTcAOperandBytes = 2 * (size_t)kTcABufBytes + 128;
 
 // One op of a tile pass (128 bytes, copied into shared memory as words).
 struct TileOpDev {
@@ -87,7 +83,7 @@ struct TileArgs {
   const void *tables;
 };
 
-size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages, int tc);
+size_t tile_smem_bytes(int prec, int t, int L, int ndata, int nops, int nstages);
 int launch_tile(qvmg_state s, const TileArgs &args);
 
 }  // namespace qvmg
