@@ -71,6 +71,9 @@ def parse():
                     help="timed samples of the CPU baseline (about 6 s each at 30 qubits)")
     ap.add_argument("--no-32q-plain", action="store_true",
                     help="skip the plain FP64 kernels at 32 qubits (about 80 s)")
+    ap.add_argument("--case", default=None, choices=sorted(PROFILE_CASES),
+                    help="run one small workload of a kernel family and exit (for ncu "
+                         "captures; prints a one-line summary, not the bench line)")
     return ap.parse_args()
 
 
@@ -656,10 +659,88 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _case_state(n, prec, seed=7):
+    from qvm_gb300 import CudaPureState, Program, circuits
+    s = CudaPureState(n, prec)
+    p = Program()
+    p.add_gates(circuits.random_su_circuit(n, depth=2, seed=seed))
+    p.plan(n, prec, fused=True, fusion_width=2)
+    p.run(s, fused=True)
+    p.free()
+    s.sync()
+    return s
+
+
+def case_sampler():
+    """26-qubit FP64 state, 4096 shots: k_block_sums, k_scan_inclusive, k_sample."""
+    s = _case_state(26, "fp64")
+    draws = np.random.default_rng(1).random(4096)
+    for _ in range(2):
+        s.sample(draws, rule="cdf")
+    s.free()
+    return "sampled 2 x 4096 shots from a 26-qubit FP64 state"
+
+
+def case_collapse():
+    """26-qubit FP64 state: P(q=1) then force-measurement: k_prob_sum_*, k_collapse."""
+    s = _case_state(26, "fp64")
+    for q in (3, 20):
+        p1 = s.excited_probability(q)
+        s.force_measurement(1, q, p1)
+    s.sync()
+    s.free()
+    return "two force-measurements on a 26-qubit FP64 state"
+
+
+def case_perm():
+    """SWAP q1,q20 as a plain pass: 27-qubit FP32 and 26-qubit FP64 (1 GiB each): k_perm."""
+    from qvm_gb300 import CudaPureState, gates as G
+    for n, prec in ((27, "fp32"), (26, "fp64")):
+        s = CudaPureState(n, prec)
+        for _ in range(2):
+            s.apply_matrix(G.gate_matrix("SWAP"), [20, 1])
+        s.sync()
+        s.free()
+    return "SWAP q1,q20 twice on 27-qubit FP32 and 26-qubit FP64 states"
+
+
+def case_dense64():
+    """A Haar SU(4) on q3,q17 of a 26-qubit FP64 state: k_dense<double, 2>."""
+    from qvm_gb300 import CudaPureState, circuits
+    s = CudaPureState(26, "fp64")
+    rng = np.random.default_rng(2)
+    for _ in range(2):
+        s.apply_matrix(circuits.haar_special_unitary(rng, 4), [17, 3])
+    s.sync()
+    s.free()
+    return "two SU(4) on a 26-qubit FP64 state"
+
+
+def case_qaoa():
+    """64 QAOA instances (n in 12..22, p = 4, 1024 shots): k_qaoa_batch."""
+    from qvm_gb300.batch import QaoaBatch, random_qaoa_batch
+    graphs, gam, bet = random_qaoa_batch(8, [12, 14, 16, 18, 20, 22], 8, p=4, seed=4)
+    b = QaoaBatch(graphs, gam, bet)
+    draws = np.random.default_rng(4).random((len(graphs), 1024))
+    for _ in range(2):
+        b.run(draws)
+    b.free()
+    return f"2 runs of a {len(graphs)}-instance QAOA batch"
+
+
+PROFILE_CASES = {"sampler": case_sampler, "collapse": case_collapse, "perm": case_perm,
+                 "dense64": case_dense64, "qaoa": case_qaoa}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.case:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"case": args.case, "did": PROFILE_CASES[args.case]()}), flush=True)
+        return
     ws, rank, local = dist()
     import torch
     torch.cuda.set_device(local)
