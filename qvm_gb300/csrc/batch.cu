@@ -274,8 +274,11 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
         for (unsigned long long tcount = 0; tcount < ntiles; ++tcount) {
           const unsigned long long base = tcount << tb;
           __syncthreads();
+          // every 16-byte load of the tile in flight at once
           for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
-            reinterpret_cast<float4 *>(tile)[j] = reinterpret_cast<const float4 *>(psi + base)[j];
+            cp_async16(reinterpret_cast<float4 *>(tile) + j,
+                       reinterpret_cast<const float4 *>(psi + base) + j);
+          cp_async_wait_all();
           if (split && threadIdx.x < 32) {
             unsigned F[kCutSlots];
             int ch;
@@ -305,15 +308,28 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
         const int hb = n - tb, Lb = tb - hb;  // n <= 26 keeps Lb >= 0
         for (unsigned long long cidx = 0; cidx < ntiles; ++cidx) {
           __syncthreads();
-          for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x) {
-            unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
-            tile[j] = psi[(h << tb) | (cidx << Lb) | lo];
+          if (Lb >= 1) {
+            // rows of >= 2 amplitudes: 16-byte asynchronous loads, all in flight
+            for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
+              unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
+              cp_async16(tile + j, psi + ((h << tb) | (cidx << Lb) | lo));
+            }
+            cp_async_wait_all();
+          } else {
+            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
+              tile[j] = psi[((unsigned long long)j << tb) | cidx];
           }
           __syncthreads();
           tile_rx_run(tile, tb, Lb, hb, c, s);
-          for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x) {
-            unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
-            psi[(h << tb) | (cidx << Lb) | lo] = tile[j];
+          if (Lb >= 1) {
+            for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
+              unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
+              *reinterpret_cast<float4 *>(psi + ((h << tb) | (cidx << Lb) | lo)) =
+                  *reinterpret_cast<const float4 *>(tile + j);
+            }
+          } else {
+            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
+              psi[((unsigned long long)j << tb) | cidx] = tile[j];
           }
         }
       }

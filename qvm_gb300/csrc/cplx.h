@@ -244,5 +244,14 @@ __device__ __forceinline__ double prob_f64(float2 v) {
 }
 __device__ __forceinline__ double prob_f64(double2 v) { return fma(v.x, v.x, v.y * v.y); }
 
+// 16-byte asynchronous global -> shared copy (LDGSTS): every load of a tile
+// is in flight at once without holding registers; wait_all completes them.
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
 
 }  // namespace qvmg
