@@ -72,21 +72,15 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
                                               const unsigned *off, const int *sp) {
   constexpr int D = 1 << K;
   float4 *t4 = reinterpret_cast<float4 *>(tile);
-  // Each thread takes two work items per iteration (g and g + blockDim.x)
-  // and issues the loads of both before any arithmetic: twice the shared-
-  // memory loads in flight, and two independent FMA streams to interleave.
-  const unsigned stride = blockDim.x;
   if constexpr (J0 >= 0) {
     // the target on tile bit 0 is matrix bit J0: amplitudes c and c | (1 << J0)
     // share a 16-byte word.  sp[0] == 0; inject the other targets.
     const unsigned ngroups = 1u << (t - K);
-    auto base = [&](unsigned g) {
+    for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
       unsigned b = g << 1;
 #pragma unroll
       for (int s = 1; s < K; ++s) b = inject0u(b, sp[s]);
-      return b;
-    };
-    auto load = [&](unsigned b, float2 (&v)[D]) {
+      float2 v[D];
 #pragma unroll
       for (int c = 0; c < D; ++c)
         if (!((c >> J0) & 1)) {
@@ -94,8 +88,6 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
           v[c] = make_float2(w.x, w.y);
           v[c | (1 << J0)] = make_float2(w.z, w.w);
         }
-    };
-    auto apply_store = [&](unsigned b, const float2 (&v)[D]) {
       float2 o[D];
 #pragma unroll
       for (int r = 0; r < D; ++r) {
@@ -110,34 +102,21 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
           const float2 a = o[r], e = o[r | (1 << J0)];
           t4[(b | off[r]) >> 1] = make_float4(a.x, a.y, e.x, e.y);
         }
-    };
-    for (unsigned g = threadIdx.x; g < ngroups; g += 2 * stride) {
-      const bool two = g + stride < ngroups;
-      const unsigned b = base(g), b2 = base(g + stride);
-      float2 v[D], v2[D];
-      load(b, v);
-      if (two) load(b2, v2);
-      apply_store(b, v);
-      if (two) apply_store(b2, v2);
     }
   } else {
     // no target on bit 0: the groups at b and b | 1 share every 16-byte word
     const unsigned npairs = 1u << (t - K - 1);
-    auto base = [&](unsigned g) {
+    for (unsigned g = threadIdx.x; g < npairs; g += blockDim.x) {
       unsigned b = g << 1;
 #pragma unroll
       for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
-      return b;
-    };
-    auto load = [&](unsigned b, float2 (&va)[D], float2 (&vb)[D]) {
+      float2 va[D], vb[D];
 #pragma unroll
       for (int c = 0; c < D; ++c) {
         const float4 w = t4[(b | off[c]) >> 1];
         va[c] = make_float2(w.x, w.y);
         vb[c] = make_float2(w.z, w.w);
       }
-    };
-    auto apply_store = [&](unsigned b, const float2 (&va)[D], const float2 (&vb)[D]) {
 #pragma unroll
       for (int r = 0; r < D; ++r) {
         float2 a = make_float2(0.f, 0.f), e = make_float2(0.f, 0.f);
@@ -148,15 +127,6 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
         }
         t4[(b | off[r]) >> 1] = make_float4(a.x, a.y, e.x, e.y);
       }
-    };
-    for (unsigned g = threadIdx.x; g < npairs; g += 2 * stride) {
-      const bool two = g + stride < npairs;
-      const unsigned b = base(g), b2 = base(g + stride);
-      float2 va[D], vb[D], vc[D], vd[D];
-      load(b, va, vb);
-      if (two) load(b2, vc, vd);
-      apply_store(b, va, vb);
-      if (two) apply_store(b2, vc, vd);
     }
   }
 }
