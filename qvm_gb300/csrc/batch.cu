@@ -20,8 +20,9 @@
 // are complex FP32; the phase table and RX coefficients are computed in FP64.
 // Each amplitude's cut comes from a per-instance table of the edges inside
 // the low 13 bits, a constant per row for the edges inside the high bits and
-// popcounts over the cross edges (cut_split); RX is applied two qubits per
-// shared-memory sweep.
+// popcounts over the cross edges (cut_split).  RX runs in register sweeps
+// of up to four qubits (each thread holds a group of 16 amplitudes), the
+// layer's phase folded into the first sweep.
 // All spin-free: the queue is a plain atomicAdd, no CTA waits on another.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -38,7 +39,7 @@
 namespace qvmg {
 
 constexpr int kQaoaTileBits = 13;
-constexpr int kQaoaThreads = 512;
+constexpr int kQaoaThreads = 256;
 constexpr int kQaoaMaxEdges = 64;
 constexpr int kQaoaMaxLayers = 16;
 constexpr int kQaoaSubBits = 7;  // 128-amplitude CDF sub-blocks
@@ -120,53 +121,81 @@ __device__ __forceinline__ int cut_split(unsigned j, const unsigned char *cl, co
          __popc((j ^ F[2]) & M[2]) + __popc((j ^ F[3]) & M[3]);
 }
 
-__device__ __forceinline__ float2 rx_apply_lo(float2 a, float2 b, float c, float s) {
-  // row 0 of [[c, -is], [-is, c]] * (a, b)
-  return make_float2(c * a.x + s * b.y, c * a.y - s * b.x);
+// RX(2 beta) = [[c, -is], [-is, c]] on an amplitude pair (a, b); symmetric
+// in the two basis states, so the pair's order does not matter.
+__device__ __forceinline__ void rx_pair(float2 &a, float2 &b, float c, float s) {
+  const float2 x = a, y = b;
+  a = make_float2(c * x.x + s * y.y, c * x.y - s * y.x);
+  b = make_float2(c * y.x + s * x.y, c * y.y - s * x.x);
 }
 
-// RX(2 beta) on local bit `bit` of a shared-memory tile of 2^tb amplitudes.
-__device__ __forceinline__ void tile_rx(float2 *tile, int tb, int bit, float c, float s) {
-  const unsigned npairs = 1u << (tb - 1);
-  for (unsigned g = threadIdx.x; g < npairs; g += blockDim.x) {
-    unsigned lo = g & ((1u << bit) - 1u);
-    unsigned i0 = ((g >> bit) << (bit + 1)) | lo;
-    unsigned i1 = i0 | (1u << bit);
-    float2 a = tile[i0], b = tile[i1];
-    tile[i0] = rx_apply_lo(a, b, c, s);
-    tile[i1] = rx_apply_lo(b, a, c, s);
+// Where the layer's phase comes from for an amplitude of a tile: the split
+// cut (low-edge table, row constants F/ch of the tile's high part, slot
+// masks) or the edge loop over the global index.
+struct PhaseSrc {
+  const float2 *phase;
+  const unsigned char *cl, *edges;
+  unsigned F[kCutSlots], M[kCutSlots];
+  int ch, m;
+  bool split;
+  unsigned long long base;  // global index of tile element 0 (edge loop)
+  __device__ __forceinline__ float2 at(unsigned j) const {
+    const int cx = split ? cut_split(j, cl, F, M, ch) : cut_value(base + j, edges, m);
+    return phase[cx];
   }
-}
+};
 
-// RX(2 beta) on local bits a < b in one sweep: each thread takes the four
-// amplitudes of a group, applies RX on bit a and then on bit b in registers
-// (the same operations, in the same order, as two single-bit sweeps).
-__device__ __forceinline__ void tile_rx2(float2 *tile, int tb, int a, int b, float c, float s) {
-  const unsigned ngroups = 1u << (tb - 2);
+// One register sweep of a shared-memory tile of 2^tb amplitudes: every
+// thread takes groups of 2^R amplitudes spanning tile bits first ..
+// first+R-1, multiplies them by the layer's phase first when PHASE, and
+// applies RX(2 beta) on all R bits in registers.  A sweep that starts at
+// tile bit 0 spans consecutive amplitudes: each lane then visits its group's
+// members in an order XORed with its lane index, so that the lanes of a warp
+// hit distinct banks; RX is symmetric, so the butterflies pair the same
+// registers whatever the order.
+template <int R, bool PHASE>
+__device__ __forceinline__ void rx_sweep(float2 *tile, int tb, int first, float c, float s,
+                                         const PhaseSrc &ph) {
+  constexpr int G = 1 << R;
+  const unsigned rot = first == 0 ? (threadIdx.x & (unsigned)(G - 1)) : 0u;
+  const unsigned ngroups = 1u << (tb - R);
+  const unsigned lowmask = (1u << first) - 1u;
   for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
-    unsigned i = ((g >> a) << (a + 1)) | (g & ((1u << a) - 1u));
-    i = ((i >> b) << (b + 1)) | (i & ((1u << b) - 1u));
-    const unsigned ia = 1u << a, ib = 1u << b;
-    float2 v00 = tile[i], v01 = tile[i | ia], v10 = tile[i | ib], v11 = tile[i | ia | ib];
-    float2 w00 = rx_apply_lo(v00, v01, c, s), w01 = rx_apply_lo(v01, v00, c, s);
-    float2 w10 = rx_apply_lo(v10, v11, c, s), w11 = rx_apply_lo(v11, v10, c, s);
-    tile[i] = rx_apply_lo(w00, w10, c, s);
-    tile[i | ib] = rx_apply_lo(w10, w00, c, s);
-    tile[i | ia] = rx_apply_lo(w01, w11, c, s);
-    tile[i | ia | ib] = rx_apply_lo(w11, w01, c, s);
+    const unsigned b = ((g >> first) << (first + R)) | (g & lowmask);
+    float2 v[G];
+#pragma unroll
+    for (int r = 0; r < G; ++r) {
+      const unsigned j = b | ((r ^ rot) << first);
+      v[r] = tile[j];
+      if constexpr (PHASE) v[r] = cmul(v[r], ph.at(j));
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+      for (int r = 0; r < G; ++r)
+        if (!((r >> i) & 1)) rx_pair(v[r], v[r | (1 << i)], c, s);
+#pragma unroll
+    for (int r = 0; r < G; ++r) tile[b | ((r ^ rot) << first)] = v[r];
   }
 }
 
-// RX on tile bits first .. first+count-1, two bits per sweep.
+// RX on tile bits first .. first+count-1 in sweeps of up to 4 bits, the
+// phase folded into the first sweep when `phase`.
 __device__ __forceinline__ void tile_rx_run(float2 *tile, int tb, int first, int count, float c,
-                                            float s) {
-  int q = 0;
-  for (; q + 1 < count; q += 2) {
-    tile_rx2(tile, tb, first + q, first + q + 1, c, s);
-    __syncthreads();
-  }
-  if (q < count) {
-    tile_rx(tile, tb, first + q, c, s);
+                                            float s, bool phase, const PhaseSrc &ph) {
+  for (int q = 0; q < count; q += 4) {
+    const int r = count - q < 4 ? count - q : 4;
+    const bool ph_now = phase && q == 0;
+    switch (r * 2 + (ph_now ? 1 : 0)) {
+      case 2: rx_sweep<1, false>(tile, tb, first + q, c, s, ph); break;
+      case 3: rx_sweep<1, true>(tile, tb, first + q, c, s, ph); break;
+      case 4: rx_sweep<2, false>(tile, tb, first + q, c, s, ph); break;
+      case 5: rx_sweep<2, true>(tile, tb, first + q, c, s, ph); break;
+      case 6: rx_sweep<3, false>(tile, tb, first + q, c, s, ph); break;
+      case 7: rx_sweep<3, true>(tile, tb, first + q, c, s, ph); break;
+      case 8: rx_sweep<4, false>(tile, tb, first + q, c, s, ph); break;
+      default: rx_sweep<4, true>(tile, tb, first + q, c, s, ph); break;
+    }
     __syncthreads();
   }
 }
@@ -191,8 +220,8 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
   __shared__ int s_inst;
   __shared__ float s_c, s_s;
   __shared__ unsigned char s_slot[kQaoaMaxEdges];
-  __shared__ unsigned s_M[kCutSlots], s_F[kCutSlots];
-  __shared__ int s_ch, s_split;
+  __shared__ unsigned s_M[kCutSlots];
+  __shared__ int s_split;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_inst = (int)atomicAdd(A.counter, 1u);
@@ -262,11 +291,11 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
       }
       __syncthreads();
       const float c = s_c, s = s_s;
+      // a resident state has no cross or high edges: its split cut is cl[x]
+      PhaseSrc ph{phase, cl, edges, {0u, 0u, 0u, 0u}, {s_M[0], s_M[1], s_M[2], s_M[3]}, 0, m,
+                  split, 0ull};
       if (resident) {
-        for (unsigned x = threadIdx.x; x < len; x += blockDim.x)
-          tile[x] = cmul(tile[x], phase[split ? (int)cl[x] : cut_value(x, edges, m)]);
-        __syncthreads();
-        tile_rx_run(tile, n, 0, n, c, s);
+        tile_rx_run(tile, n, 0, n, c, s, true, ph);
       } else {
         const int tb = kQaoaTileBits;
         const unsigned long long ntiles = len >> tb;
@@ -279,28 +308,11 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
             cp_async16(reinterpret_cast<float4 *>(tile) + j,
                        reinterpret_cast<const float4 *>(psi + base) + j);
           cp_async_wait_all();
-          if (split && threadIdx.x < 32) {
-            unsigned F[kCutSlots];
-            int ch;
-            cut_row(tcount, edges, s_slot, m, F, ch);
-            if (threadIdx.x == 0) {
-              for (int q = 0; q < kCutSlots; ++q) s_F[q] = F[q];
-              s_ch = ch;
-            }
-          }
+          // the row constants of this tile's high part, computed by every warp
+          ph.base = base;
+          if (split) cut_row(tcount, edges, s_slot, m, ph.F, ph.ch);
           __syncthreads();
-          if (split) {
-            const unsigned F[kCutSlots] = {s_F[0], s_F[1], s_F[2], s_F[3]};
-            const unsigned M[kCutSlots] = {s_M[0], s_M[1], s_M[2], s_M[3]};
-            const int ch = s_ch;
-            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              tile[j] = cmul(tile[j], phase[cut_split(j, cl, F, M, ch)]);
-          } else {
-            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              tile[j] = cmul(tile[j], phase[cut_value(base + j, edges, m)]);
-          }
-          __syncthreads();
-          tile_rx_run(tile, tb, 0, tb, c, s);
+          tile_rx_run(tile, tb, 0, tb, c, s, true, ph);
           for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
             reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
         }
@@ -320,7 +332,7 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
               tile[j] = psi[((unsigned long long)j << tb) | cidx];
           }
           __syncthreads();
-          tile_rx_run(tile, tb, Lb, hb, c, s);
+          tile_rx_run(tile, tb, Lb, hb, c, s, false, ph);
           if (Lb >= 1) {
             for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
               unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
