@@ -16,10 +16,11 @@
 //          searched per draw by one warp, smallest x with C(x) >= draw.
 // States of <= 13 qubits live in shared memory for the whole circuit; larger
 // ones stay in HBM and are swept in two tile passes per layer (low 13 qubits
-// contiguous; then the high qubits with a 2^(26-n)-amplitude row), each
-// streaming its tiles through two shared-memory buffers so that the next
-// tile loads while the current one is swept; layer 0's first pass makes its
-// uniform tiles in place instead of reading an initialised state.  Amplitudes
+// contiguous; then the high qubits with a 2^(26-n)-amplitude row); layer
+// 0's first pass makes its uniform tiles in place instead of reading an
+// initialised state.  (Streaming tiles through two buffers per CTA was
+// measured too: its 128 KiB of buffers leave one CTA per SM, and the
+// 4096-instance batch went from 143 to 199 ms.)  Amplitudes
 // are complex FP32; the phase table and RX coefficients are computed in FP64.
 // Each amplitude's cut comes from a per-instance table of the edges inside
 // the low 13 bits, a constant per row for the edges inside the high bits and
@@ -42,15 +43,10 @@
 namespace qvmg {
 
 constexpr int kQaoaTileBits = 13;
-constexpr int kQaoaThreads = 512;
+constexpr int kQaoaThreads = 256;
 constexpr int kQaoaMaxEdges = 64;
 constexpr int kQaoaMaxLayers = 16;
 constexpr int kQaoaSubBits = 7;  // 128-amplitude CDF sub-blocks
-// Dynamic shared memory: two tile buffers (a state held in HBM streams its
-// next tile into one while the other is swept), the layer's phase table,
-// the edges and the low-edge cut table.
-constexpr int kQaoaSmemBytes = 2 * (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 +
-                               2 * kQaoaMaxEdges + (1 << kQaoaTileBits) + 16;
 
 struct QaoaInst {
   unsigned long long state_off;  // float2 offset of the state
@@ -218,10 +214,10 @@ __device__ __forceinline__ double prob_d(float2 v) {
   return (double)v.x * (double)v.x + (double)v.y * (double)v.y;
 }
 
-__global__ void __launch_bounds__(kQaoaThreads, 1) k_qaoa_batch(const __grid_constant__ QaoaArgs A) {
+__global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_constant__ QaoaArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  float2 *tile = reinterpret_cast<float2 *>(smem);                     // 2 x 2^13
-  float2 *phase = tile + 2 * (1u << kQaoaTileBits);                     // kQaoaMaxEdges+1
+  float2 *tile = reinterpret_cast<float2 *>(smem);                     // 2^13
+  float2 *phase = tile + (1u << kQaoaTileBits);                         // kQaoaMaxEdges+1
   unsigned char *edges = reinterpret_cast<unsigned char *>(phase + kQaoaMaxEdges + 1);
   unsigned char *cl = edges + 2 * kQaoaMaxEdges;                        // 2^13 low-edge cuts
   __shared__ double red[kQaoaThreads / 32];
@@ -278,7 +274,7 @@ __global__ void __launch_bounds__(kQaoaThreads, 1) k_qaoa_batch(const __grid_con
     const float amp0 = (float)(1.0 / sqrt((double)len));
     const bool resident = n <= kQaoaTileBits;
     // H on all qubits: a resident state starts in the tile; a state in HBM
-    // is never written uniform -- layer 0's first pass fills its tiles
+    // is never written uniform -- layer 0's first pass makes its tiles
     if (resident)
       for (unsigned x = threadIdx.x; x < len; x += blockDim.x) tile[x] = make_float2(amp0, 0.f);
     for (int l = 0; l < A.p; ++l) {
@@ -305,77 +301,54 @@ __global__ void __launch_bounds__(kQaoaThreads, 1) k_qaoa_batch(const __grid_con
       } else {
         const int tb = kQaoaTileBits;
         const unsigned long long ntiles = len >> tb;
-        float2 *const buf[2] = {tile, tile + (1u << tb)};
-        // Both passes stream tiles through two buffers: the loads of tile
-        // i+1 (16-byte asynchronous copies, one commit group per tile) are
-        // in flight while tile i is swept and stored.
-        // pass A: contiguous tiles, phase + RX on qubits 0..12 (layer 0
-        // fills its tiles with the uniform amplitude instead of loading)
-        const bool fill = l == 0;
-        auto issue_a = [&](unsigned long long tcount, float2 *dst) {
-          const float4 *src = reinterpret_cast<const float4 *>(psi + (tcount << tb));
-          for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
-            cp_async16(reinterpret_cast<float4 *>(dst) + j, src + j);
-        };
+        // pass A: contiguous tiles, phase + RX on qubits 0..12
         for (unsigned long long tcount = 0; tcount < ntiles; ++tcount) {
           const unsigned long long base = tcount << tb;
-          float2 *cur = buf[tcount & 1], *nxt = buf[(tcount + 1) & 1];
-          __syncthreads();  // the previous tile's stores have read `nxt`
-          if (fill) {
+          __syncthreads();
+          if (l == 0) {
             for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              cur[j] = make_float2(amp0, 0.f);
+              tile[j] = make_float2(amp0, 0.f);
           } else {
-            if (tcount == 0) {
-              issue_a(0, cur);
-              cp_async_commit();
-            }
-            if (tcount + 1 < ntiles) issue_a(tcount + 1, nxt);
-            cp_async_commit();
-            cp_async_wait_group1();  // tile tcount has landed
+            // every 16-byte load of the tile in flight at once
+            for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
+              cp_async16(reinterpret_cast<float4 *>(tile) + j,
+                         reinterpret_cast<const float4 *>(psi + base) + j);
+            cp_async_wait_all();
           }
           // the row constants of this tile's high part, computed by every warp
           ph.base = base;
           if (split) cut_row(tcount, edges, s_slot, m, ph.F, ph.ch);
           __syncthreads();
-          tile_rx_run(cur, tb, 0, tb, c, s, true, ph);
+          tile_rx_run(tile, tb, 0, tb, c, s, true, ph);
           for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
-            reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(cur)[j];
+            reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
         }
         // pass B: rows of 2^Lb amplitudes, the high qubits 13..n-1 in the tile
         const int hb = n - tb, Lb = tb - hb;  // n <= 26 keeps Lb >= 0
-        auto issue_b = [&](unsigned long long cidx, float2 *dst) {
-          for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
-            unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
-            cp_async16(dst + j, psi + ((h << tb) | (cidx << Lb) | lo));
-          }
-        };
         for (unsigned long long cidx = 0; cidx < ntiles; ++cidx) {
-          float2 *cur = buf[cidx & 1], *nxt = buf[(cidx + 1) & 1];
           __syncthreads();
           if (Lb >= 1) {
-            // rows of >= 2 amplitudes: 16-byte asynchronous loads
-            if (cidx == 0) {
-              issue_b(0, cur);
-              cp_async_commit();
+            // rows of >= 2 amplitudes: 16-byte asynchronous loads, all in flight
+            for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
+              unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
+              cp_async16(tile + j, psi + ((h << tb) | (cidx << Lb) | lo));
             }
-            if (cidx + 1 < ntiles) issue_b(cidx + 1, nxt);
-            cp_async_commit();
-            cp_async_wait_group1();
+            cp_async_wait_all();
           } else {
             for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              cur[j] = psi[((unsigned long long)j << tb) | cidx];
+              tile[j] = psi[((unsigned long long)j << tb) | cidx];
           }
           __syncthreads();
-          tile_rx_run(cur, tb, Lb, hb, c, s, false, ph);
+          tile_rx_run(tile, tb, Lb, hb, c, s, false, ph);
           if (Lb >= 1) {
             for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
               unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
               *reinterpret_cast<float4 *>(psi + ((h << tb) | (cidx << Lb) | lo)) =
-                  *reinterpret_cast<const float4 *>(cur + j);
+                  *reinterpret_cast<const float4 *>(tile + j);
             }
           } else {
             for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              psi[((unsigned long long)j << tb) | cidx] = cur[j];
+              psi[((unsigned long long)j << tb) | cidx] = tile[j];
           }
         }
       }
@@ -615,7 +588,8 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
   static std::once_flag attr_once;
   static cudaError_t attr_err = cudaSuccess;
   e = once(attr_once, attr_err, [] {
-    const int bytes = kQaoaSmemBytes;
+    const int bytes = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges +
+                      (1 << kQaoaTileBits) + 16;
     return cudaFuncSetAttribute(k_qaoa_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
   if (e != cudaSuccess) {
@@ -689,8 +663,9 @@ int qvmg_qaoa_batch_run(qvmg_qaoa_batch b, const double *draws, int nshots, doub
     cudaGraph_t g;
     QVMG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(b->counter, 0, sizeof(unsigned int), b->stream);
-    int smem = kQaoaSmemBytes;
-    int grid = std::min(b->ninst, sm_count());
+    int smem = (1 << kQaoaTileBits) * 8 + (kQaoaMaxEdges + 1) * 8 + 2 * kQaoaMaxEdges +
+               (1 << kQaoaTileBits) + 16;
+    int grid = std::min(b->ninst, sm_count() * 3);
     k_qaoa_batch<<<grid, kQaoaThreads, smem, b->stream>>>(A);
     cudaError_t le = cudaGetLastError();
     cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
