@@ -357,6 +357,42 @@ def run_plain_passes(runs: int = 5, seed: int = 9):
     return out
 
 
+def run_engines_other(runs: int = 2):
+    """The FP32 tile engines on circuits other than the headline: the
+    config-1 family (H, then RX/RZ on every qubit and CNOTs on alternating
+    pairs per layer) at 28 qubits with 10 layers, and the QFT at 30 qubits.
+    Each runs fused with the FMA engine (fusion width 2, 13-qubit tiles) and
+    with the tensor-core engine (fusion width 4, 12-qubit tiles); device ms
+    per run from per-pass events, plus the plan's tensor-core block count."""
+    from qvm_gb300 import CudaPureState, Program, circuits
+    from qvm_gb300.autotune import apply_engine
+    out = {}
+    for name, n, gates in (("layers28", 28, circuits.random_layers(28, layers=10, seed=1)),
+                           ("qft30", 30, circuits.qft(30))):
+        s = CudaPureState(n, "fp32")
+        row = {"qubits": n, "gates": len(gates)}
+        for engine, fw, tile in (("fma", 2, 13), ("tc", 4, 12)):
+            p = Program()
+            p.add_gates(gates)
+            apply_engine(p, engine)
+            st = p.plan(n, "fp32", fused=True, fusion_width=fw, tile_qubits=tile)
+            best = float("inf")
+            for _ in range(runs + 1):
+                s.set_to_zero_state()
+                ms, _ = p.run_profiled(s, fused=True)
+                best = min(best, float(ms.sum()))
+            row[engine] = {"ms": best, "passes": st["passes"], "fusion_width": fw,
+                           "tile_qubits": tile}
+            if engine == "tc":
+                d = p.describe()
+                row[engine]["tc_blocks"] = sum(1 for ps in d["passes"] if ps["kind"] == "tile"
+                                               for op in ps["ops"] if op["kind"] == "tc")
+            p.free()
+        s.free()
+        out[name] = row
+    return out
+
+
 def run_layers_shots(n: int = 20, layers: int = 10, shots: int = 1000, seed: int = 1, runs: int = 5):
     """The plain small case: 20-qubit FP64 state, H on all qubits, 10 layers of
     RX/RZ on every qubit and CNOTs on alternating pairs, then measure-all for
@@ -944,6 +980,7 @@ def main():
         result["plain_passes"] = run_plain_passes()
     if not args.no_layers and rank == 0:
         result["layers20_shots"] = run_layers_shots()
+        result["engines_other"] = run_engines_other()
     if not args.no_endpoints and rank == 0:
         result["endpoints"] = run_endpoints()
     if not args.no_batch and rank == 0:

@@ -205,26 +205,43 @@ __global__ void __launch_bounds__(256)
 }
 
 // Inclusive prefix scan in place over n doubles, one CTA of 1024 threads.
+// The array is walked in coalesced tiles of 1024 consecutive entries: each
+// tile is scanned by warp shuffles and a scan of the 32 warp totals, shifted
+// by the running total of the tiles before it; the next tile's load is issued
+// before the current one is scanned.  (The block-sum array is at most 2^18+1
+// entries for a 30-qubit state, 2 MiB, and stays in L2.)
 __global__ void __launch_bounds__(1024) k_scan_inclusive(double *__restrict__ x, uint64_t n) {
-  __shared__ double sh[1024];
-  const uint64_t per = (n + blockDim.x - 1) / blockDim.x;
-  const uint64_t lo = threadIdx.x * per;
-  const uint64_t hi = min(n, lo + per);
-  double s = 0.0;
-  for (uint64_t i = lo; i < hi; ++i) s += x[i];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  // Hillis-Steele inclusive scan over the 1024 chunk totals.
-  for (int off = 1; off < 1024; off <<= 1) {
-    double add = threadIdx.x >= (unsigned)off ? sh[threadIdx.x - off] : 0.0;
+  __shared__ double warp_tot[32];
+  __shared__ double carry_sh;
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double carry = 0.0;
+  double next = threadIdx.x < n ? x[threadIdx.x] : 0.0;
+  for (uint64_t base = 0; base < n; base += 1024) {
+    const uint64_t i = base + threadIdx.x;
+    double v = next;
+    next = base + 1024 + threadIdx.x < n ? x[base + 1024 + threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= (unsigned)o) v += y;
+    }
+    if (lane == 31) warp_tot[warp] = v;
     __syncthreads();
-    sh[threadIdx.x] += add;
+    if (warp == 0) {
+      double t = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= (unsigned)o) t += y;
+      }
+      warp_tot[lane] = t;  // inclusive scan of the warp totals
+      if (lane == 31) carry_sh = t;
+    }
     __syncthreads();
-  }
-  double run = threadIdx.x ? sh[threadIdx.x - 1] : 0.0;
-  for (uint64_t i = lo; i < hi; ++i) {
-    run += x[i];
-    x[i] = run;
+    const double before = warp ? warp_tot[warp - 1] : 0.0;
+    if (i < n) x[i] = carry + (before + v);
+    carry += carry_sh;
+    __syncthreads();  // warp_tot and carry_sh are rewritten by the next tile
   }
 }
 
