@@ -125,12 +125,21 @@ __device__ __forceinline__ int cut_split(unsigned j, const unsigned char *cl, co
          __popc((j ^ F[2]) & M[2]) + __popc((j ^ F[3]) & M[3]);
 }
 
-// RX(2 beta) = [[c, -is], [-is, c]] on an amplitude pair (a, b); symmetric
+// RX(2 beta) = [[c, -is], [-is, c]] with its larger coefficient factored
+// out: c (I - i t X), t = tan(beta), when |c| >= |s| (KFORM false), else
+// s (k I - i X), k = cot(beta).  The factor (c^n or s^n for the n qubits)
+// goes into the layer's phase table, so a pair costs four FMAs.  Symmetric
 // in the two basis states, so the pair's order does not matter.
-__device__ __forceinline__ void rx_pair(float2 &a, float2 &b, float c, float s) {
+template <bool KFORM>
+__device__ __forceinline__ void rx_pair(float2 &a, float2 &b, float w) {
   const float2 x = a, y = b;
-  a = make_float2(c * x.x + s * y.y, c * x.y - s * y.x);
-  b = make_float2(c * y.x + s * x.y, c * y.y - s * x.x);
+  if constexpr (KFORM) {
+    a = make_float2(fmaf(w, x.x, y.y), fmaf(w, x.y, -y.x));
+    b = make_float2(fmaf(w, y.x, x.y), fmaf(w, y.y, -x.x));
+  } else {
+    a = make_float2(fmaf(w, y.y, x.x), fmaf(-w, y.x, x.y));
+    b = make_float2(fmaf(w, x.y, y.x), fmaf(-w, x.x, y.y));
+  }
 }
 
 // Where the layer's phase comes from for an amplitude of a tile: the split
@@ -157,8 +166,8 @@ struct PhaseSrc {
 // members in an order XORed with its lane index, so that the lanes of a warp
 // hit distinct banks; RX is symmetric, so the butterflies pair the same
 // registers whatever the order.
-template <int R, bool PHASE>
-__device__ __forceinline__ void rx_sweep(float2 *tile, int tb, int first, float c, float s,
+template <int R, bool PHASE, bool KFORM>
+__device__ __forceinline__ void rx_sweep(float2 *tile, int tb, int first, float w,
                                          const PhaseSrc &ph) {
   constexpr int G = 1 << R;
   const unsigned rot = first == 0 ? (threadIdx.x & (unsigned)(G - 1)) : 0u;
@@ -177,7 +186,7 @@ __device__ __forceinline__ void rx_sweep(float2 *tile, int tb, int first, float 
     for (int i = 0; i < R; ++i)
 #pragma unroll
       for (int r = 0; r < G; ++r)
-        if (!((r >> i) & 1)) rx_pair(v[r], v[r | (1 << i)], c, s);
+        if (!((r >> i) & 1)) rx_pair<KFORM>(v[r], v[r | (1 << i)], w);
 #pragma unroll
     for (int r = 0; r < G; ++r) tile[b | ((r ^ rot) << first)] = v[r];
   }
@@ -185,23 +194,30 @@ __device__ __forceinline__ void rx_sweep(float2 *tile, int tb, int first, float 
 
 // RX on tile bits first .. first+count-1 in sweeps of up to 4 bits, the
 // phase folded into the first sweep when `phase`.
-__device__ __forceinline__ void tile_rx_run(float2 *tile, int tb, int first, int count, float c,
-                                            float s, bool phase, const PhaseSrc &ph) {
+template <bool KFORM>
+__device__ __forceinline__ void tile_rx_run_f(float2 *tile, int tb, int first, int count, float w,
+                                              bool phase, const PhaseSrc &ph) {
   for (int q = 0; q < count; q += 4) {
     const int r = count - q < 4 ? count - q : 4;
     const bool ph_now = phase && q == 0;
     switch (r * 2 + (ph_now ? 1 : 0)) {
-      case 2: rx_sweep<1, false>(tile, tb, first + q, c, s, ph); break;
-      case 3: rx_sweep<1, true>(tile, tb, first + q, c, s, ph); break;
-      case 4: rx_sweep<2, false>(tile, tb, first + q, c, s, ph); break;
-      case 5: rx_sweep<2, true>(tile, tb, first + q, c, s, ph); break;
-      case 6: rx_sweep<3, false>(tile, tb, first + q, c, s, ph); break;
-      case 7: rx_sweep<3, true>(tile, tb, first + q, c, s, ph); break;
-      case 8: rx_sweep<4, false>(tile, tb, first + q, c, s, ph); break;
-      default: rx_sweep<4, true>(tile, tb, first + q, c, s, ph); break;
+      case 2: rx_sweep<1, false, KFORM>(tile, tb, first + q, w, ph); break;
+      case 3: rx_sweep<1, true, KFORM>(tile, tb, first + q, w, ph); break;
+      case 4: rx_sweep<2, false, KFORM>(tile, tb, first + q, w, ph); break;
+      case 5: rx_sweep<2, true, KFORM>(tile, tb, first + q, w, ph); break;
+      case 6: rx_sweep<3, false, KFORM>(tile, tb, first + q, w, ph); break;
+      case 7: rx_sweep<3, true, KFORM>(tile, tb, first + q, w, ph); break;
+      case 8: rx_sweep<4, false, KFORM>(tile, tb, first + q, w, ph); break;
+      default: rx_sweep<4, true, KFORM>(tile, tb, first + q, w, ph); break;
     }
     __syncthreads();
   }
+}
+
+__device__ __forceinline__ void tile_rx_run(float2 *tile, int tb, int first, int count, float w,
+                                            bool kform, bool phase, const PhaseSrc &ph) {
+  if (kform) tile_rx_run_f<true>(tile, tb, first, count, w, phase, ph);
+  else tile_rx_run_f<false>(tile, tb, first, count, w, phase, ph);
 }
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -222,7 +238,6 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
   unsigned char *cl = edges + 2 * kQaoaMaxEdges;                        // 2^13 low-edge cuts
   __shared__ double red[kQaoaThreads / 32];
   __shared__ int s_inst;
-  __shared__ float s_c, s_s;
   __shared__ unsigned char s_slot[kQaoaMaxEdges];
   __shared__ unsigned s_M[kCutSlots];
   __shared__ int s_split;
@@ -280,24 +295,24 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
     for (int l = 0; l < A.p; ++l) {
       const double g = A.gammas[I.param_off + l], b = A.betas[I.param_off + l];
       __syncthreads();
+      // RX(2 beta) with its larger coefficient factored out (rx_pair); the
+      // factor for all n qubits scales the layer's phase table
+      double rs, rc;
+      sincos(b, &rs, &rc);
+      const bool kform = fabs(rs) > fabs(rc);
+      const double fac = pow(kform ? rs : rc, (double)n);
       for (int c = threadIdx.x; c <= m; c += blockDim.x) {
         double sn, cs;
         sincos(-g * (double)(m - 2 * c) * 0.5, &sn, &cs);
-        phase[c] = make_float2((float)cs, (float)sn);
-      }
-      if (threadIdx.x == 0) {
-        double sn, cs;
-        sincos(b, &sn, &cs);
-        s_c = (float)cs;
-        s_s = (float)sn;
+        phase[c] = make_float2((float)(fac * cs), (float)(fac * sn));
       }
       __syncthreads();
-      const float c = s_c, s = s_s;
+      const float w = (float)(kform ? rc / rs : rs / rc);
       // a resident state has no cross or high edges: its split cut is cl[x]
       PhaseSrc ph{phase, cl, edges, {0u, 0u, 0u, 0u}, {s_M[0], s_M[1], s_M[2], s_M[3]}, 0, m,
                   split, 0ull};
       if (resident) {
-        tile_rx_run(tile, n, 0, n, c, s, true, ph);
+        tile_rx_run(tile, n, 0, n, w, kform, true, ph);
       } else {
         const int tb = kQaoaTileBits;
         const unsigned long long ntiles = len >> tb;
@@ -319,7 +334,7 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
           ph.base = base;
           if (split) cut_row(tcount, edges, s_slot, m, ph.F, ph.ch);
           __syncthreads();
-          tile_rx_run(tile, tb, 0, tb, c, s, true, ph);
+          tile_rx_run(tile, tb, 0, tb, w, kform, true, ph);
           for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
             reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
         }
@@ -339,7 +354,7 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
               tile[j] = psi[((unsigned long long)j << tb) | cidx];
           }
           __syncthreads();
-          tile_rx_run(tile, tb, Lb, hb, c, s, false, ph);
+          tile_rx_run(tile, tb, Lb, hb, w, kform, false, ph);
           if (Lb >= 1) {
             for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
               unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
