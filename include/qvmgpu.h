@@ -331,6 +331,32 @@ int qvmg_qaoa_batch_state(qvmg_qaoa_batch b, int instance, double *amps);
 uint64_t qvmg_qaoa_batch_bytes(qvmg_qaoa_batch b);
 int qvmg_qaoa_batch_free(qvmg_qaoa_batch b);
 
+/* ---- batches of small programs (one persistent launch) ------------------- */
+/* Many small, uneven programs run in one launch, each from |0...0> on its own
+ * state: the per-request program runs of the reference's server
+ * (app/src/api/multishot.lisp:87-101, app/src/handle-request.lisp) and
+ * sample-wavefunction-multiple-times (src/measurement.lisp:246-288) for each
+ * program.  Program i has nqubits[i] qubits (1..13 in QVMG_FP32, 1..12 in
+ * QVMG_FP64), nops[i] dense gates and nshots[i] shots.  Gates are given in
+ * order, all programs concatenated: op_k[] their widths (1..3), op_qubits[]
+ * their nat-tuple qubits (k per gate), matrices[] their row-major 2^k x 2^k
+ * complex matrices as interleaved doubles.  A program runs on one CTA, so its
+ * results do not depend on the other programs of the batch. */
+typedef struct qvmg_sbatch_s *qvmg_sbatch;
+int qvmg_sbatch_create(int precision, int nprograms, const int *nqubits, const int *nops,
+                       const int *op_k, const int *op_qubits, const double *matrices,
+                       const int *nshots, qvmg_sbatch *out);
+/* Run every program; draws (the programs' shots concatenated, each in [0, 1])
+ * give the samples, written to shots[] as basis-state indices: the smallest i
+ * with C(i) >= draw (FP32 states: draw times the state's total probability). */
+int qvmg_sbatch_run(qvmg_sbatch b, const double *draws, uint64_t *shots);
+/* Where program i's draws and shots start in the concatenated arrays. */
+int qvmg_sbatch_shot_offset(qvmg_sbatch b, int program, uint64_t *offset);
+/* Program i's final state as complex128 (after a run). */
+int qvmg_sbatch_state(qvmg_sbatch b, int program, double *amps);
+uint64_t qvmg_sbatch_bytes(qvmg_sbatch b);
+int qvmg_sbatch_free(qvmg_sbatch b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,12 @@ SIGNATURES = {
     "qvmg_qaoa_batch_state": (_i, [_vp, _i, _dp]),
     "qvmg_qaoa_batch_bytes": (_u64, [_vp]),
     "qvmg_qaoa_batch_free": (_i, [_vp]),
+    "qvmg_sbatch_create": (_i, [_i, _i, _ip, _ip, _ip, _ip, _dp, _ip, _vpp]),
+    "qvmg_sbatch_run": (_i, [_vp, _dp, _u64p]),
+    "qvmg_sbatch_shot_offset": (_i, [_vp, _i, _u64p]),
+    "qvmg_sbatch_state": (_i, [_vp, _i, _dp]),
+    "qvmg_sbatch_bytes": (_u64, [_vp]),
+    "qvmg_sbatch_free": (_i, [_vp]),
 }
 
 STATUS = {

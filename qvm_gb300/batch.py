@@ -1,4 +1,5 @@
-"""Batched QAOA MaxCut instances (one persistent launch for many circuits).
+"""Batched circuits in one persistent launch: QAOA MaxCut instances, and
+batches of arbitrary small programs.
 
 Mirrors the QAOA workload of the reference's examples/qaoa.lisp:7-206 (H on
 all qubits, p layers of ZZ(gamma) on graph edges and RX(2 beta) on all
@@ -67,6 +68,71 @@ class QaoaBatch:
     def free(self):
         if self._h:
             L.call("qvmg_qaoa_batch_free", self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class ProgramBatch:
+    """Many small programs (gate lists on 1..13 qubits in FP32, 1..12 in
+    FP64) run from |0...0> in one persistent launch, each with its own
+    shots.  programs: list of (n, gates, nshots), gates a list of
+    (matrix, nat-tuple qubits) with 1- to 3-qubit matrices."""
+
+    def __init__(self, programs, precision: str = "fp64"):
+        from .state import PRECISIONS
+        self.nprog = len(programs)
+        self.n = np.array([int(n) for n, _, _ in programs], dtype=np.int32)
+        self.nshots = np.array([int(k) for _, _, k in programs], dtype=np.int32)
+        nops = np.array([len(g) for _, g, _ in programs], dtype=np.int32)
+        ks, qs, ms = [], [], []
+        for _, gates, _ in programs:
+            for m, q in gates:
+                ks.append(len(q))
+                qs.extend(int(x) for x in q)
+                ms.append(np.asarray(m, dtype=np.complex128).ravel())
+        op_k = np.array(ks or [0], dtype=np.int32)
+        op_q = np.array(qs or [0], dtype=np.int32)
+        mats = np.concatenate(ms) if ms else np.zeros(1, dtype=np.complex128)
+        mats = np.ascontiguousarray(mats.view(np.float64))
+        ip = ctypes.POINTER(ctypes.c_int)
+        self._h = ctypes.c_void_p()
+        L.call("qvmg_sbatch_create", PRECISIONS[precision], self.nprog,
+               self.n.ctypes.data_as(ip), nops.ctypes.data_as(ip), op_k.ctypes.data_as(ip),
+               op_q.ctypes.data_as(ip), mats.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+               self.nshots.ctypes.data_as(ip), ctypes.byref(self._h))
+        self.offsets = []
+        off = ctypes.c_uint64()
+        for i in range(self.nprog):
+            L.call("qvmg_sbatch_shot_offset", self._h, i, ctypes.byref(off))
+            self.offsets.append(int(off.value))
+
+    def run(self, draws):
+        """draws: one array per program (its nshots uniforms).  Returns the
+        list of per-program shot index arrays."""
+        flat = np.concatenate([np.asarray(d, dtype=np.float64).ravel() for d in draws]) \
+            if self.nprog else np.zeros(0)
+        if len(flat) != int(self.nshots.sum()):
+            raise ValueError("one draw per shot of every program is required")
+        flat = np.ascontiguousarray(flat)
+        out = np.zeros(max(1, len(flat)), dtype=np.uint64)
+        L.call("qvmg_sbatch_run", self._h, flat.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+               out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+        return [out[o:o + int(k)].copy() for o, k in zip(self.offsets, self.nshots)]
+
+    def state(self, i: int) -> np.ndarray:
+        out = np.zeros(1 << int(self.n[i]), dtype=np.complex128)
+        L.call("qvmg_sbatch_state", self._h, int(i),
+               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return out
+
+    def free(self):
+        if self._h:
+            L.call("qvmg_sbatch_free", self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

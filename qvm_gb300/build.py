@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libqvmgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["state.cu", "gates.cu", "measure.cu", "tile.cu", "program.cu", "plan.cpp",
-           "batch.cu", "endpoints.cu", "noise.cu"]
+           "batch.cu", "sbatch.cu", "endpoints.cu", "noise.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
               "-Wall", "--expt-relaxed-constexpr", "-I", INCLUDE]
