@@ -785,9 +785,10 @@ def case_dense64():
 
 
 def case_qaoa():
-    """64 QAOA instances (n in 12..22, p = 4, 1024 shots): k_qaoa_batch."""
+    """152 QAOA instances of 20 qubits (p = 4, 1024 shots; one per SM of
+    the launch's grid, 1.2 GB of states): k_qaoa_batch."""
     from qvm_gb300.batch import QaoaBatch, random_qaoa_batch
-    graphs, gam, bet = random_qaoa_batch(8, [12, 14, 16, 18, 20, 22], 8, p=4, seed=4)
+    graphs, gam, bet = random_qaoa_batch(19, [20], 8, p=4, seed=4)
     b = QaoaBatch(graphs, gam, bet)
     draws = np.random.default_rng(4).random((len(graphs), 1024))
     for _ in range(2):
