@@ -35,6 +35,14 @@ import numpy as np
 
 from .state import CudaPureState, Program, state_bytes
 
+# States this small run as programs of a ProgramBatch: one persistent
+# launch for every such request of a precision waiting at that moment.
+SMALL_MAX_QUBITS = {"fp32": 13, "fp64": 12}
+
+
+def is_small(req) -> bool:
+    return req.n <= SMALL_MAX_QUBITS[req.precision] and all(len(q) <= 3 for _, q in req.gates)
+
 
 @dataclass
 class Request:
@@ -102,12 +110,17 @@ class StatePool:
 class Server:
     def __init__(self, hbm_budget: float = 180e9, workers: int = 16, aging_s: float = 2.0,
                  fast_workers: int = 8, fast_cost: float = 1000.0 * (1 << 24),
-                 reserve_pool: bool = True):
+                 reserve_pool: bool = True, small_batch: int = 64):
         """`workers` take any request; `fast_workers` more take only requests
         whose estimated cost (gates x 2^n, FP64 x 8) is at most `fast_cost`
         (by default a 1000-gate 24-qubit FP32 program), so that a small
         request never waits for a worker held by a multi-second job.
-        `reserve_pool` maps the budget into the device memory pool at start."""
+        `reserve_pool` maps the budget into the device memory pool at start.
+        A worker that admits a small request (<= 13 qubits in FP32, <= 12 in
+        FP64, gates of <= 3 qubits) takes up to `small_batch` - 1 more small
+        requests of that precision from the queue and runs them all as one
+        ProgramBatch launch (0: every request runs on its own state)."""
+        self.small_batch = int(small_batch)
         self.budget = int(hbm_budget)
         self.aging_s = float(aging_s)
         self.fast_cost = float(fast_cost)
@@ -200,6 +213,9 @@ class Server:
                     continue
                 return
             req, fut, need, st = item
+            if self.small_batch > 0 and is_small(req):
+                self._run_small_batch(req, fut, need, st)
+                continue
             t0 = time.perf_counter()
             try:
                 if st is None:
@@ -234,6 +250,48 @@ class Server:
                 else:
                     self.reserved -= need
                 self.cv.notify_all()
+
+    def _run_small_batch(self, req, fut, need, st):
+        """Run `req` with the small requests of its precision that are still
+        queued (up to small_batch in all) as one ProgramBatch launch."""
+        from .batch import ProgramBatch
+        group = [(req, fut, need)]
+        with self.cv:
+            keep = collections.deque()
+            while self.queue:
+                item = self.queue.popleft()
+                r = item[0]
+                if (len(group) < self.small_batch and r.precision == req.precision
+                        and is_small(r) and self.reserved + item[2] <= self.budget):
+                    group.append(item)
+                    self.reserved += item[2]
+                else:
+                    keep.append(item)
+            self.queue = keep
+        t0 = time.perf_counter()
+        try:
+            draws = [r.draws if r.draws is not None else np.random.default_rng(0).random(r.shots)
+                     for r, _, _ in group]
+            b = ProgramBatch([(r.n, r.gates, r.shots) for r, _, _ in group], req.precision)
+            try:
+                shots = b.run(draws)
+            finally:
+                b.free()
+            t1 = time.perf_counter()
+            for (r, f, _), sh in zip(group, shots):
+                f.set_result(Result(sh, t0 - r.arrival, t1 - t0, t1 - r.arrival, r.tag))
+        except Exception as e:  # the batch's requests fail, the server keeps going
+            for _, f, _ in group:
+                if not f.done():
+                    f.set_exception(e)
+        with self.cv:
+            if st is not None:
+                self.pool.give(st, req.precision)   # the admitted state stays pooled
+            else:
+                self.reserved -= need
+            for _, _, nd in group[1:]:
+                self.reserved -= nd
+            self.cv.notify_all()
 
     def close_now(self):
         """Cancel the queued requests, let running ones finish, free states."""

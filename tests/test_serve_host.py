@@ -113,7 +113,7 @@ def test_workers_lanes_eviction_and_priority(monkeypatch):
     budget = 3 * state_bytes(20, "fp64")
     fast_cost = 200.0 * (1 << 14)
     srv = Server(hbm_budget=budget, workers=3, fast_workers=2, fast_cost=fast_cost,
-                 reserve_pool=False)
+                 reserve_pool=False, small_batch=0)
     rng = np.random.default_rng(8)
     reqs = []
     for i in range(60):
@@ -161,7 +161,7 @@ def test_failed_request_frees_its_program(monkeypatch):
     _FakeState.lock = threading.Lock()
     _FakeState.live = _FakeState.peak = 0
     srv = Server(hbm_budget=4 * state_bytes(14, "fp64"), workers=2, fast_workers=0,
-                 reserve_pool=False)
+                 reserve_pool=False, small_batch=0)
     bad = srv.submit(Request(12, [None] * 13, 4, "fp64", np.zeros(4), True, "bad"))
     good = srv.submit(Request(12, [None] * 5, 4, "fp64", np.zeros(4), True, "good"))
     with pytest.raises(RuntimeError, match="planted"):
@@ -170,3 +170,47 @@ def test_failed_request_frees_its_program(monkeypatch):
     srv.close()
     assert _Counting.made == 2 and _Counting.freed == 2
     assert _FakeState.live == 0
+
+
+def test_small_requests_run_as_batches(monkeypatch):
+    """Small requests waiting together run as one ProgramBatch per precision
+    (a fake here): every request gets its own program's shots, large ones
+    keep their own states, and the budget returns to zero."""
+    import threading
+    from qvm_gb300 import batch, serve
+
+    calls = []
+
+    class _FakeBatch:
+        def __init__(self, programs, precision):
+            self.programs, self.precision = programs, precision
+            calls.append((len(programs), precision))
+
+        def run(self, draws):
+            time.sleep(0.01)
+            return [np.full(k, n * 1000 + len(g), dtype=np.uint64)
+                    for (n, g, k) in self.programs]
+
+        def free(self):
+            pass
+
+    monkeypatch.setattr(batch, "ProgramBatch", _FakeBatch)
+    monkeypatch.setattr(serve, "CudaPureState", _FakeState)
+    monkeypatch.setattr(serve, "Program", _FakeProgram)
+    _FakeState.lock = threading.Lock()
+    _FakeState.live = _FakeState.peak = 0
+    srv = Server(hbm_budget=4 * state_bytes(20, "fp64"), workers=1, fast_workers=0,
+                 reserve_pool=False, small_batch=8)
+    g1 = [(np.eye(2), [0])]
+    reqs = [Request(20, [None] * 3, 2, "fp32", np.zeros(2), True, "big")]
+    reqs += [Request(10 + i % 3, g1 * (i + 1), 3, "fp32" if i % 2 else "fp64", np.zeros(3),
+                     True, f"s{i}") for i in range(12)]
+    futs = [(r, srv.submit(r)) for r in reqs]
+    for r, f in futs:
+        res = f.result(timeout=30)
+        if r.tag != "big":
+            assert (res.shots == r.n * 1000 + len(r.gates)).all(), r.tag
+    srv.close()
+    assert sum(c for c, _ in calls) == 12 and len(calls) < 12   # batched, both precisions
+    assert {p for _, p in calls} == {"fp32", "fp64"}
+    assert srv.reserved == 0
