@@ -444,11 +444,12 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 // and commits them to an mbarrier that the data warps wait on with a
 // bounded loop.
 //
-// Chunks are software-pipelined over two TMEM buffers (each D | A) and two
-// barriers: while the MMAs of chunk c run, the data warps read out and
-// scatter chunk c-1 and gather chunk c+1.
-constexpr int kTcCols = 128;           // TMEM columns per CTA: 2 buffers of 64
-constexpr int kTcBufCols = 64;         // D in [0, 32), A in [32, 64)
+// Chunks go in batches of up to four, each chunk with its own TMEM buffer
+// (D | A): a batch is gathered, its MMAs issued together under one commit,
+// and read out after one wait -- two barriers per batch.
+constexpr int kTcBufs = 4;             // chunks per batch (TMEM buffers)
+constexpr int kTcBufCols = 64;         // per buffer: D in [0, 32), A in [32, 64)
+constexpr int kTcCols = kTcBufs * kTcBufCols;  // TMEM columns per CTA
 constexpr int kTcACol = 32;
 constexpr int kTcWaitLimit = 1 << 22;  // polls of an MMA barrier before giving up
 
@@ -586,17 +587,24 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
     return b;
   };
-  for (unsigned ch = 0; ch <= nchunks; ++ch) {
-    const uint32_t buf = ctx.tmem + (ch & 1u) * kTcBufCols;
-    if (!issuer && ch < nchunks) {
-      // gather + split chunk ch into this buffer's A columns (its previous
-      // MMAs, chunk ch-2, completed and were read out last iteration)
-      const unsigned b = group_base(ch);
-      uint32_t hi[H], lo[H];
+  // Chunks go in batches of up to kTcBufs: the data warps gather and split a
+  // whole batch into its TMEM buffers, one barrier hands it to the issuing
+  // warp, which issues every chunk's MMAs (each chunk on its own
+  // accumulator) under one commit, and the data warps read out and scatter
+  // the batch after one wait.  Two barriers per batch, the MMAs of all its
+  // chunks in flight together.
+  for (unsigned base = 0; base < nchunks; base += kTcBufs) {
+    const unsigned nb = nchunks - base < (unsigned)kTcBufs ? nchunks - base : (unsigned)kTcBufs;
+    if (!issuer) {
+      for (unsigned c = 0; c < nb; ++c) {
+        const uint32_t buf = ctx.tmem + c * kTcBufCols;
+        const unsigned b = group_base(base + c);
+        uint32_t hi[H], lo[H];
 #pragma unroll
-      for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
-      tmem_st<H>(buf + lanes + kTcACol + half * H, hi);
-      tmem_st<H>(buf + lanes + kTcACol + D + half * H, lo);
+        for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
+        tmem_st<H>(buf + lanes + kTcACol + half * H, hi);
+        tmem_st<H>(buf + lanes + kTcACol + D + half * H, lo);
+      }
       asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -604,45 +612,55 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (*abort_flag) {  // uniform: read after the barrier
       ctx.ok = 0;
+      ctx.phase[0] ^= 1u;  // back to the phase of the commit that was not seen
       return;
     }
     if (issuer) {
-      if (ch < nchunks && lane == 0) {
-        const uint32_t a = buf + kTcACol;
+      if (lane == 0) {
+        for (unsigned c = 0; c < nb; ++c) {
+          const uint32_t buf = ctx.tmem + c * kTcBufCols;
+          const uint32_t a = buf + kTcACol;
 #pragma unroll
-        for (int s = 0; s < kSteps; ++s)  // Ahi * Bhi
-          tc_mma(buf, a + 8 * s, tc_desc(bhi + s * 256, kSboB), idesc, s > 0);
+          for (int s = 0; s < kSteps; ++s)  // Ahi * Bhi
+            tc_mma(buf, a + 8 * s, tc_desc(bhi + s * 256, kSboB), idesc, s > 0);
 #pragma unroll
-        for (int s = 0; s < kSteps; ++s)  // + Alo * Bhi
-          tc_mma(buf, a + D + 8 * s, tc_desc(bhi + s * 256, kSboB), idesc, 1);
+          for (int s = 0; s < kSteps; ++s)  // + Alo * Bhi
+            tc_mma(buf, a + D + 8 * s, tc_desc(bhi + s * 256, kSboB), idesc, 1);
 #pragma unroll
-        for (int s = 0; s < kSteps; ++s)  // + Ahi * Blo
-          tc_mma(buf, a + 8 * s, tc_desc(bhi + kPieceB + s * 256, kSboB), idesc, 1);
+          for (int s = 0; s < kSteps; ++s)  // + Ahi * Blo
+            tc_mma(buf, a + 8 * s, tc_desc(bhi + kPieceB + s * 256, kSboB), idesc, 1);
+        }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                ctx.mbar[ch & 1u])
+                ctx.mbar[0])
             : "memory");
       }
-    } else if (ch >= 1) {
-      // read out and scatter chunk ch-1 while chunk ch's MMAs are issued
-      const unsigned pb = (ch - 1) & 1u;
-      if (!tc_wait(ctx.mbar[pb], ctx.phase[pb])) {
+    } else {
+      if (!tc_wait(ctx.mbar[0], ctx.phase[0])) {
         *abort_flag = 1;  // seen by every thread after the next barrier
-        continue;
-      }
-      ctx.phase[pb] ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      uint32_t r[D];
-      tmem_ld<D>(ctx.tmem + pb * kTcBufCols + lanes + half * D, r);
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      const unsigned b = group_base(ch - 1);
+      } else {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        for (unsigned c = 0; c < nb; ++c) {
+          uint32_t r[D];
+          tmem_ld<D>(ctx.tmem + c * kTcBufCols + lanes + half * D, r);
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+          const unsigned b = group_base(base + c);
 #pragma unroll
-      for (int i = 0; i < H; ++i)
-        tile[b | off[i]] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+          for (int i = 0; i < H; ++i)
+            tile[b | off[i]] =
+                make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+        }
+      }
     }
+    ctx.phase[0] ^= 1u;  // every thread: the barrier's next phase
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();  // the batch's buffers are read out before the next one is written
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   }
-  __syncthreads();  // a wait that gave up on the last chunk is seen here
-  if (*abort_flag) ctx.ok = 0;
+  if (*abort_flag) {  // a wait that gave up on the last batch (seen after its barrier)
+    ctx.ok = 0;
+    ctx.phase[0] ^= 1u;
+  }
 }
 
 // ---- double-float ops (fused FP64 tiles) -----------------------------------------
@@ -928,7 +946,6 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
       if (threadIdx.x == 0) atomicExch(p.status, 1);
       // let MMAs still in flight finish (bounded) before their TMEM is freed
       (void)tc_wait(ctx.mbar[0], ctx.phase[0]);
-      (void)tc_wait(ctx.mbar[1], ctx.phase[1]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
