@@ -444,13 +444,14 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 // and commits them to an mbarrier that the data warps wait on with a
 // bounded loop.
 //
-// Chunks go in batches of up to four, each chunk with its own TMEM buffer
-// (D | A): a batch is gathered, its MMAs issued together under one commit,
-// and read out after one wait -- two barriers per batch.
-constexpr int kTcBufs = 4;             // chunks per batch (TMEM buffers)
-constexpr int kTcBufCols = 64;         // per buffer: D in [0, 32), A in [32, 64)
-constexpr int kTcCols = kTcBufs * kTcBufCols;  // TMEM columns per CTA
-constexpr int kTcACol = 32;
+// Chunks go in batches (four for 4-qubit blocks, eight for 3-qubit ones),
+// each chunk with its own TMEM buffer (D | A): a batch is gathered, its MMAs
+// issued together under one commit, and read out after one wait -- two
+// barriers per batch.
+constexpr int kTcCols = 256;  // TMEM columns per CTA
+// A chunk of a k-qubit block takes 4 * 2^k TMEM columns: D (2^(k+1) FP32
+// outputs) then A (2^k columns of hi, 2^k of lo, bf16 pairs); a batch is as
+// many chunks as the CTA's columns hold (4 for k = 4, 8 for k = 3).
 constexpr int kTcWaitLimit = 1 << 22;  // polls of an MMA barrier before giving up
 
 struct TcCtx {
@@ -549,7 +550,8 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
   constexpr uint32_t kSboB = 2 * 16 * D;   // Bt rows hold 2D bf16 (4D bytes); 8 rows per group
   constexpr uint32_t kPieceB = 8 * D * D;  // bytes of Bt hi (then Bt lo)
   constexpr int kSteps = NC / 16;          // 16-element K steps per piece (8 TMEM columns)
-  static_assert(NC <= kTcACol && 2 * D <= kTcBufCols - kTcACol, "TMEM buffer layout");
+  constexpr int kBufCols = 4 * D, kACol = 2 * D;  // per chunk: D | A hi | A lo
+  constexpr unsigned kBufs = kTcCols / kBufCols;  // chunks per batch
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool issuer = warp == kTileThreads / 32;  // the extra warp issues the MMAs
   const int sub = warp & 3, half = (warp >> 2) & 1;
@@ -587,23 +589,23 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
     return b;
   };
-  // Chunks go in batches of up to kTcBufs: the data warps gather and split a
+  // Chunks go in batches of up to kBufs: the data warps gather and split a
   // whole batch into its TMEM buffers, one barrier hands it to the issuing
   // warp, which issues every chunk's MMAs (each chunk on its own
   // accumulator) under one commit, and the data warps read out and scatter
   // the batch after one wait.  Two barriers per batch, the MMAs of all its
   // chunks in flight together.
-  for (unsigned base = 0; base < nchunks; base += kTcBufs) {
-    const unsigned nb = nchunks - base < (unsigned)kTcBufs ? nchunks - base : (unsigned)kTcBufs;
+  for (unsigned base = 0; base < nchunks; base += kBufs) {
+    const unsigned nb = nchunks - base < kBufs ? nchunks - base : kBufs;
     if (!issuer) {
       for (unsigned c = 0; c < nb; ++c) {
-        const uint32_t buf = ctx.tmem + c * kTcBufCols;
+        const uint32_t buf = ctx.tmem + c * kBufCols;
         const unsigned b = group_base(base + c);
         uint32_t hi[H], lo[H];
 #pragma unroll
         for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
-        tmem_st<H>(buf + lanes + kTcACol + half * H, hi);
-        tmem_st<H>(buf + lanes + kTcACol + D + half * H, lo);
+        tmem_st<H>(buf + lanes + kACol + half * H, hi);
+        tmem_st<H>(buf + lanes + kACol + D + half * H, lo);
       }
       asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
     }
@@ -618,8 +620,8 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     if (issuer) {
       if (lane == 0) {
         for (unsigned c = 0; c < nb; ++c) {
-          const uint32_t buf = ctx.tmem + c * kTcBufCols;
-          const uint32_t a = buf + kTcACol;
+          const uint32_t buf = ctx.tmem + c * kBufCols;
+          const uint32_t a = buf + kACol;
 #pragma unroll
           for (int s = 0; s < kSteps; ++s)  // Ahi * Bhi
             tc_mma(buf, a + 8 * s, tc_desc(bhi + s * 256, kSboB), idesc, s > 0);
@@ -642,7 +644,7 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         for (unsigned c = 0; c < nb; ++c) {
           uint32_t r[D];
-          tmem_ld<D>(ctx.tmem + c * kTcBufCols + lanes + half * D, r);
+          tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r);
           asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
           const unsigned b = group_base(base + c);
 #pragma unroll
