@@ -583,12 +583,15 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
   const uint32_t lanes = (uint32_t)(sub * 32) << 16;
   const uint32_t bhi = smem_u32(bmat);
   const unsigned nchunks = (1u << (t - K)) / kTileTcRows;
-  auto group_base = [&](unsigned ch) {
-    unsigned b = ch * kTileTcRows + sub * 32 + lane;
+  // Inserting the block's zero bits is linear over disjoint bit sets, so a
+  // group's base is this thread's row part OR the chunk part (computed once).
+  auto inject_all = [&](unsigned x) {
 #pragma unroll
-    for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
-    return b;
+    for (int s = 0; s < K; ++s) x = inject0u(x, sp[s]);
+    return x;
   };
+  const unsigned row_base = inject_all((unsigned)(sub * 32 + lane));
+  auto group_base = [&](unsigned ch) { return row_base | inject_all(ch * kTileTcRows); };
   // Chunks go in batches of up to kBufs: the data warps gather and split a
   // whole batch into its TMEM buffers, one barrier hands it to the issuing
   // warp, which issues every chunk's MMAs (each chunk on its own
