@@ -452,7 +452,7 @@ constexpr int kTcCols = 256;  // TMEM columns per CTA
 // A chunk of a k-qubit block takes 4 * 2^k TMEM columns: D (2^(k+1) FP32
 // outputs) then A (2^k columns of hi, 2^k of lo, bf16 pairs); a batch is as
 // many chunks as the CTA's columns hold (4 for k = 4, 8 for k = 3).
-constexpr int kTcWaitLimit = 1 << 22;  // polls of an MMA barrier before giving up
+constexpr int kTcWaitLimit = 1 << 20;  // tries of an MMA barrier wait before giving up
 
 struct TcCtx {
   uint32_t tmem;      // TMEM address of lane 0, column 0 of this CTA's allocation
@@ -520,14 +520,17 @@ __device__ __forceinline__ void tmem_ld<16>(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 // Bounded wait for the barrier phase of parity `phase`; 1 when it completed.
+// Each try may suspend the thread for up to 1 us until the phase completes
+// (instead of spinning on issue slots the other CTA of the SM could use), so
+// the whole wait gives up after at most ~1 s.
 __device__ __forceinline__ uint32_t tc_wait(uint32_t mbar, uint32_t phase) {
   uint32_t done = 0;
   for (int it = 0; it < kTcWaitLimit && !done; ++it)
     asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         "selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(mbar), "r"(phase)
+        : "r"(mbar), "r"(phase), "r"(1000u)
         : "memory");
   return done;
 }
