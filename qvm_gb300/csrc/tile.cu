@@ -445,20 +445,24 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 // bounded loop.
 //
 // Chunks go in batches (four for 4-qubit blocks, eight for 3-qubit ones),
-// each chunk with its own TMEM buffer (D | A): a batch is gathered, its MMAs
-// issued together under one commit, and read out after one wait -- two
-// barriers per batch.
+// each chunk with its own TMEM buffer (D | A), completion barrier and named
+// CTA barrier for the hand-over to the issuing warp, so that the MMAs of one
+// chunk overlap the data warps' work on the others.
 constexpr int kTcCols = 256;  // TMEM columns per CTA
 // A chunk of a k-qubit block takes 4 * 2^k TMEM columns: D (2^(k+1) FP32
 // outputs) then A (2^k columns of hi, 2^k of lo, bf16 pairs); a batch is as
 // many chunks as the CTA's columns hold (4 for k = 4, 8 for k = 3).
 constexpr int kTcWaitLimit = 1 << 20;  // tries of an MMA barrier wait before giving up
 
+constexpr int kTcMaxBufs = 8;  // chunks of a batch: one TMEM buffer, barrier pair each
+
 struct TcCtx {
-  uint32_t tmem;      // TMEM address of lane 0, column 0 of this CTA's allocation
-  uint32_t mbar[2];   // shared addresses of the two MMA-completion barriers
-  uint32_t phase[2];  // parity of the phase each barrier's next wait is for
-  int ok;             // 0 once a wait gave up
+  uint32_t tmem;       // TMEM address of lane 0, column 0 of this CTA's allocation
+  uint32_t mbar;       // shared address of the first of kTcMaxBufs MMA-completion barriers
+  uint32_t phases;     // bit c: parity of the phase barrier c's next wait is for
+  int ok;              // 0 once a wait gave up
+  uint32_t last_bar;   // the latest batch's last barrier and the parity it completes
+  uint32_t last_par;   // (a kernel that gave up waits for it before freeing TMEM)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -595,14 +599,19 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
   };
   const unsigned row_base = inject_all((unsigned)(sub * 32 + lane));
   auto group_base = [&](unsigned ch) { return row_base | inject_all(ch * kTileTcRows); };
-  // Chunks go in batches of up to kBufs: the data warps gather and split a
-  // whole batch into its TMEM buffers, one barrier hands it to the issuing
-  // warp, which issues every chunk's MMAs (each chunk on its own
-  // accumulator) under one commit, and the data warps read out and scatter
-  // the batch after one wait.  Two barriers per batch, the MMAs of all its
-  // chunks in flight together.
+  // Chunks go in batches of up to kBufs, each chunk with its own TMEM buffer,
+  // completion barrier and named CTA barrier (id 1 + c).  The data warps
+  // gather and split chunk c, then arrive on its named barrier without
+  // waiting and go on to chunk c+1; the issuing warp syncs on that barrier,
+  // issues chunk c's MMAs and commits them to barrier c.  The data warps then
+  // read the chunks out in order, each after its own commit: the MMAs of a
+  // chunk overlap the gathers of the later chunks and the readout of the
+  // earlier ones.  One CTA-wide barrier per op.
+  static_assert(kTcCols / (4 * 8) <= kTcMaxBufs, "barriers per batch");
   for (unsigned base = 0; base < nchunks; base += kBufs) {
     const unsigned nb = nchunks - base < kBufs ? nchunks - base : kBufs;
+    ctx.last_bar = ctx.mbar + 8 * (nb - 1);
+    ctx.last_par = (ctx.phases >> (nb - 1)) & 1u;
     if (!issuer) {
       for (unsigned c = 0; c < nb; ++c) {
         const uint32_t buf = ctx.tmem + c * kBufCols;
@@ -612,20 +621,33 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
         for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
         tmem_st<H>(buf + lanes + kACol + half * H, hi);
         tmem_st<H>(buf + lanes + kACol + D + half * H, lo);
+        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        asm volatile("bar.arrive %0, %1;\n" ::"r"(1u + c), "n"(kTileThreads + 32) : "memory");
       }
-      asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (*abort_flag) {  // uniform: read after the barrier
-      ctx.ok = 0;
-      ctx.phase[0] ^= 1u;  // back to the phase of the commit that was not seen
-      return;
-    }
-    if (issuer) {
-      if (lane == 0) {
-        for (unsigned c = 0; c < nb; ++c) {
+      for (unsigned c = 0; c < nb; ++c) {
+        const uint32_t par = (ctx.phases >> c) & 1u;
+        ctx.phases ^= 1u << c;
+        if (!ctx.ok) continue;  // gave up on an earlier chunk: no more reads
+        if (!tc_wait(ctx.mbar + 8 * c, par)) {
+          *abort_flag = 1;  // seen by every thread after the op's barrier
+          ctx.ok = 0;
+          continue;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        uint32_t r[D];
+        tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r);
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        const unsigned b = group_base(base + c);
+#pragma unroll
+        for (int i = 0; i < H; ++i)
+          tile[b | off[i]] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+      }
+    } else {
+      for (unsigned c = 0; c < nb; ++c) {
+        asm volatile("bar.sync %0, %1;\n" ::"r"(1u + c), "n"(kTileThreads + 32) : "memory");
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (lane == 0) {
           const uint32_t buf = ctx.tmem + c * kBufCols;
           const uint32_t a = buf + kACol;
 #pragma unroll
@@ -637,38 +659,19 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
 #pragma unroll
           for (int s = 0; s < kSteps; ++s)  // + Ahi * Blo
             tc_mma(buf, a + 8 * s, tc_desc(bhi + kPieceB + s * 256, kSboB), idesc, 1);
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                  ctx.mbar + 8 * c)
+              : "memory");
         }
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                ctx.mbar[0])
-            : "memory");
-      }
-    } else {
-      if (!tc_wait(ctx.mbar[0], ctx.phase[0])) {
-        *abort_flag = 1;  // seen by every thread after the next barrier
-      } else {
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        for (unsigned c = 0; c < nb; ++c) {
-          uint32_t r[D];
-          tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r);
-          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-          const unsigned b = group_base(base + c);
-#pragma unroll
-          for (int i = 0; i < H; ++i)
-            tile[b | off[i]] =
-                make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
-        }
+        ctx.phases ^= 1u << c;
       }
     }
-    ctx.phase[0] ^= 1u;  // every thread: the barrier's next phase
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();  // the batch's buffers are read out before the next one is written
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   }
-  if (*abort_flag) {  // a wait that gave up on the last batch (seen after its barrier)
-    ctx.ok = 0;
-    ctx.phase[0] ^= 1u;
-  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();  // the op's outputs are in the tile; a wait that gave up is seen here
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (*abort_flag) ctx.ok = 0;
 }
 
 // ---- double-float ops (fused FP64 tiles) -----------------------------------------
@@ -825,10 +828,10 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     k_tile(typename GT<T>::G *__restrict__ a, const __grid_constant__ TileArgs p) {
   using C = typename CT<T>::C;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ __align__(8) unsigned long long tc_mbar[2];
+  __shared__ __align__(8) unsigned long long tc_mbar[kTcMaxBufs];
   __shared__ uint32_t tc_tmem_slot;
   __shared__ int tc_abort;
-  TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1};
+  TcCtx ctx{0u, 0u, 0u, 1, 0u, 0u};
   if constexpr (RB < 0) {
     if ((threadIdx.x >> 5) == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -839,8 +842,9 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     }
     if (threadIdx.x == 0) {
       tc_abort = 0;
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[0])) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[1])) : "memory");
+      for (int c = 0; c < kTcMaxBufs; ++c)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[c]))
+                     : "memory");
       asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
   }
@@ -876,8 +880,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     ctx.tmem = tc_tmem_slot;
-    ctx.mbar[0] = smem_u32(&tc_mbar[0]);
-    ctx.mbar[1] = smem_u32(&tc_mbar[1]);
+    ctx.mbar = smem_u32(&tc_mbar[0]);
   }
   constexpr int per16 = 16 / sizeof(C);  // amplitudes per 16-byte chunk
   const unsigned nchunks = (1u << t) / per16;
@@ -953,7 +956,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     if (!ctx.ok) {
       if (threadIdx.x == 0) atomicExch(p.status, 1);
       // let MMAs still in flight finish (bounded) before their TMEM is freed
-      (void)tc_wait(ctx.mbar[0], ctx.phase[0]);
+      (void)tc_wait(ctx.last_bar, ctx.last_par);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
