@@ -64,11 +64,11 @@ struct Pass {
 };
 
 // Device descriptor sizes of tile ops and stages (tile.h), and the dynamic
-// shared memory one tile pass may use (227 KiB per CTA on sm_103a, less 64
+// shared memory one tile pass may use (227 KiB per CTA on sm_103a, less 128
 // bytes for the kernel's static shared variables).
 constexpr size_t kTileOpDescBytes = 128;
 constexpr size_t kTileStageDescBytes = 80;
-constexpr size_t kTileSmemBudget = 227 * 1024 - 64;
+constexpr size_t kTileSmemBudget = 227 * 1024 - 128;
 size_t tile_pass_smem_bytes(const Pass &p, int prec);
 
 // Register bits per thread for a tile of t qubits run by 256 threads:

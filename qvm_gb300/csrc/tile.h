@@ -16,8 +16,8 @@ constexpr int kTileThreads = 256;  // register-stage and tensor-core kernels
 // took the fused 28-qubit circuit from 522 to 537 ms.
 constexpr int kTileThreadsSmem = 128;
 // Dynamic shared memory of a tile pass: the 227 KiB a CTA may hold, less
-// 64 bytes for the kernel's static shared variables (MMA barrier, TMEM slot).
-constexpr int kTileMaxSmem = 227 * 1024 - 64;
+// 128 bytes for the kernel's static shared variables (MMA barriers, TMEM slot).
+constexpr int kTileMaxSmem = 227 * 1024 - 128;
 constexpr int kTileMaxE = 24;
 constexpr int kTileTcRows = 128;  // groups per tensor-core chunk (MMA M)
 
