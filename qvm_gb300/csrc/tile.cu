@@ -599,19 +599,18 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
   };
   const unsigned row_base = inject_all((unsigned)(sub * 32 + lane));
   auto group_base = [&](unsigned ch) { return row_base | inject_all(ch * kTileTcRows); };
-  // Chunks go in batches of up to kBufs, each chunk with its own TMEM buffer,
-  // completion barrier and named CTA barrier (id 1 + c).  The data warps
-  // gather and split chunk c, then arrive on its named barrier without
-  // waiting and go on to chunk c+1; the issuing warp syncs on that barrier,
-  // issues chunk c's MMAs and commits them to barrier c.  The data warps then
-  // read the chunks out in order, each after its own commit: the MMAs of a
-  // chunk overlap the gathers of the later chunks and the readout of the
-  // earlier ones.  One CTA-wide barrier per op.
-  static_assert(kTcCols / (4 * 8) <= kTcMaxBufs, "barriers per batch");
+  // Chunks go in batches of up to kBufs, each chunk with its own TMEM buffer.
+  // The data warps gather, split and store a whole batch into tensor memory
+  // with one wait for all its stores (TMEM stores and loads have long
+  // latency: waiting chunk by chunk cost ~10 % of the pass), one CTA barrier
+  // hands the batch to the issuing warp, which issues every chunk's MMAs
+  // under one commit, and the data warps read the batch out two chunks per
+  // wait.  Two CTA barriers per batch.
+  static_assert(kTcCols / (4 * 8) <= kTcMaxBufs, "chunks per batch");
   for (unsigned base = 0; base < nchunks; base += kBufs) {
     const unsigned nb = nchunks - base < kBufs ? nchunks - base : kBufs;
-    ctx.last_bar = ctx.mbar + 8 * (nb - 1);
-    ctx.last_par = (ctx.phases >> (nb - 1)) & 1u;
+    ctx.last_bar = ctx.mbar;
+    ctx.last_par = ctx.phases & 1u;
     if (!issuer) {
       for (unsigned c = 0; c < nb; ++c) {
         const uint32_t buf = ctx.tmem + c * kBufCols;
@@ -621,33 +620,22 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
         for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
         tmem_st<H>(buf + lanes + kACol + half * H, hi);
         tmem_st<H>(buf + lanes + kACol + D + half * H, lo);
-        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        asm volatile("bar.arrive %0, %1;\n" ::"r"(1u + c), "n"(kTileThreads + 32) : "memory");
       }
-      for (unsigned c = 0; c < nb; ++c) {
-        const uint32_t par = (ctx.phases >> c) & 1u;
-        ctx.phases ^= 1u << c;
-        if (!ctx.ok) continue;  // gave up on an earlier chunk: no more reads
-        if (!tc_wait(ctx.mbar + 8 * c, par)) {
-          *abort_flag = 1;  // seen by every thread after the op's barrier
-          ctx.ok = 0;
-          continue;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        uint32_t r[D];
-        tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r);
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        const unsigned b = group_base(base + c);
-#pragma unroll
-        for (int i = 0; i < H; ++i)
-          tile[b | off[i]] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
-      }
-    } else {
-      for (unsigned c = 0; c < nb; ++c) {
-        asm volatile("bar.sync %0, %1;\n" ::"r"(1u + c), "n"(kTileThreads + 32) : "memory");
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        if (lane == 0) {
+      asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (*abort_flag) {  // uniform: read after the barrier
+      ctx.ok = 0;
+      ctx.last_par ^= 1u;  // the previous batch's commit is the one that may be in flight
+      return;
+    }
+    const uint32_t par = ctx.phases & 1u;
+    ctx.phases ^= 1u;  // every thread: the barrier's next phase
+    if (issuer) {
+      if (lane == 0) {
+        for (unsigned c = 0; c < nb; ++c) {
           const uint32_t buf = ctx.tmem + c * kBufCols;
           const uint32_t a = buf + kACol;
 #pragma unroll
@@ -659,19 +647,40 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
 #pragma unroll
           for (int s = 0; s < kSteps; ++s)  // + Ahi * Blo
             tc_mma(buf, a + 8 * s, tc_desc(bhi + kPieceB + s * 256, kSboB), idesc, 1);
-          asm volatile(
-              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                  ctx.mbar + 8 * c)
-              : "memory");
         }
-        ctx.phases ^= 1u << c;
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                ctx.mbar)
+            : "memory");
+      }
+    } else if (!tc_wait(ctx.mbar, par)) {
+      *abort_flag = 1;  // seen by every thread after the next barrier
+    } else {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      for (unsigned c = 0; c < nb; c += 2) {
+        const bool two = c + 1 < nb;
+        uint32_t r0[D], r1[D];
+        tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r0);
+        if (two) tmem_ld<D>(ctx.tmem + (c + 1) * kBufCols + lanes + half * D, r1);
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        const unsigned b0 = group_base(base + c);
+#pragma unroll
+        for (int i = 0; i < H; ++i)
+          tile[b0 | off[i]] = make_float2(__uint_as_float(r0[2 * i]), __uint_as_float(r0[2 * i + 1]));
+        if (two) {
+          const unsigned b1 = group_base(base + c + 1);
+#pragma unroll
+          for (int i = 0; i < H; ++i)
+            tile[b1 | off[i]] =
+                make_float2(__uint_as_float(r1[2 * i]), __uint_as_float(r1[2 * i + 1]));
+        }
       }
     }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();  // the batch's buffers are read out before the next one is written
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();  // the op's outputs are in the tile; a wait that gave up is seen here
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  if (*abort_flag) ctx.ok = 0;
+  if (*abort_flag) ctx.ok = 0;  // a wait that gave up (seen after its barrier)
 }
 
 // ---- double-float ops (fused FP64 tiles) -----------------------------------------
