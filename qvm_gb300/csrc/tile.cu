@@ -445,24 +445,20 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 // bounded loop.
 //
 // Chunks go in batches (four for 4-qubit blocks, eight for 3-qubit ones),
-// each chunk with its own TMEM buffer (D | A), completion barrier and named
-// CTA barrier for the hand-over to the issuing warp, so that the MMAs of one
-// chunk overlap the data warps' work on the others.
+// each chunk with its own TMEM buffer (D | A): a batch is gathered, its MMAs
+// issued together under one commit, and read out after one wait -- two
+// barriers per batch.
 constexpr int kTcCols = 256;  // TMEM columns per CTA
 // A chunk of a k-qubit block takes 4 * 2^k TMEM columns: D (2^(k+1) FP32
 // outputs) then A (2^k columns of hi, 2^k of lo, bf16 pairs); a batch is as
 // many chunks as the CTA's columns hold (4 for k = 4, 8 for k = 3).
 constexpr int kTcWaitLimit = 1 << 20;  // tries of an MMA barrier wait before giving up
 
-constexpr int kTcMaxBufs = 8;  // chunks of a batch: one TMEM buffer, barrier pair each
-
 struct TcCtx {
-  uint32_t tmem;       // TMEM address of lane 0, column 0 of this CTA's allocation
-  uint32_t mbar;       // shared address of the first of kTcMaxBufs MMA-completion barriers
-  uint32_t phases;     // bit c: parity of the phase barrier c's next wait is for
-  int ok;              // 0 once a wait gave up
-  uint32_t last_bar;   // the latest batch's last barrier and the parity it completes
-  uint32_t last_par;   // (a kernel that gave up waits for it before freeing TMEM)
+  uint32_t tmem;      // TMEM address of lane 0, column 0 of this CTA's allocation
+  uint32_t mbar[2];   // shared addresses of the two MMA-completion barriers
+  uint32_t phase[2];  // parity of the phase each barrier's next wait is for
+  int ok;             // 0 once a wait gave up
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -599,18 +595,14 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
   };
   const unsigned row_base = inject_all((unsigned)(sub * 32 + lane));
   auto group_base = [&](unsigned ch) { return row_base | inject_all(ch * kTileTcRows); };
-  // Chunks go in batches of up to kBufs, each chunk with its own TMEM buffer.
-  // The data warps gather, split and store a whole batch into tensor memory
-  // with one wait for all its stores (TMEM stores and loads have long
-  // latency: waiting chunk by chunk cost ~10 % of the pass), one CTA barrier
-  // hands the batch to the issuing warp, which issues every chunk's MMAs
-  // under one commit, and the data warps read the batch out two chunks per
-  // wait.  Two CTA barriers per batch.
-  static_assert(kTcCols / (4 * 8) <= kTcMaxBufs, "chunks per batch");
+  // Chunks go in batches of up to kBufs: the data warps gather and split a
+  // whole batch into its TMEM buffers, one barrier hands it to the issuing
+  // warp, which issues every chunk's MMAs (each chunk on its own
+  // accumulator) under one commit, and the data warps read out and scatter
+  // the batch after one wait.  Two barriers per batch, the MMAs of all its
+  // chunks in flight together.
   for (unsigned base = 0; base < nchunks; base += kBufs) {
     const unsigned nb = nchunks - base < kBufs ? nchunks - base : kBufs;
-    ctx.last_bar = ctx.mbar;
-    ctx.last_par = ctx.phases & 1u;
     if (!issuer) {
       for (unsigned c = 0; c < nb; ++c) {
         const uint32_t buf = ctx.tmem + c * kBufCols;
@@ -628,11 +620,9 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (*abort_flag) {  // uniform: read after the barrier
       ctx.ok = 0;
-      ctx.last_par ^= 1u;  // the previous batch's commit is the one that may be in flight
+      ctx.phase[0] ^= 1u;  // back to the phase of the commit that was not seen
       return;
     }
-    const uint32_t par = ctx.phases & 1u;
-    ctx.phases ^= 1u;  // every thread: the barrier's next phase
     if (issuer) {
       if (lane == 0) {
         for (unsigned c = 0; c < nb; ++c) {
@@ -650,37 +640,35 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
         }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                ctx.mbar)
+                ctx.mbar[0])
             : "memory");
       }
-    } else if (!tc_wait(ctx.mbar, par)) {
-      *abort_flag = 1;  // seen by every thread after the next barrier
     } else {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      for (unsigned c = 0; c < nb; c += 2) {
-        const bool two = c + 1 < nb;
-        uint32_t r0[D], r1[D];
-        tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r0);
-        if (two) tmem_ld<D>(ctx.tmem + (c + 1) * kBufCols + lanes + half * D, r1);
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        const unsigned b0 = group_base(base + c);
-#pragma unroll
-        for (int i = 0; i < H; ++i)
-          tile[b0 | off[i]] = make_float2(__uint_as_float(r0[2 * i]), __uint_as_float(r0[2 * i + 1]));
-        if (two) {
-          const unsigned b1 = group_base(base + c + 1);
+      if (!tc_wait(ctx.mbar[0], ctx.phase[0])) {
+        *abort_flag = 1;  // seen by every thread after the next barrier
+      } else {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        for (unsigned c = 0; c < nb; ++c) {
+          uint32_t r[D];
+          tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r);
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+          const unsigned b = group_base(base + c);
 #pragma unroll
           for (int i = 0; i < H; ++i)
-            tile[b1 | off[i]] =
-                make_float2(__uint_as_float(r1[2 * i]), __uint_as_float(r1[2 * i + 1]));
+            tile[b | off[i]] =
+                make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
         }
       }
     }
+    ctx.phase[0] ^= 1u;  // every thread: the barrier's next phase
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();  // the batch's buffers are read out before the next one is written
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   }
-  if (*abort_flag) ctx.ok = 0;  // a wait that gave up (seen after its barrier)
+  if (*abort_flag) {  // a wait that gave up on the last batch (seen after its barrier)
+    ctx.ok = 0;
+    ctx.phase[0] ^= 1u;
+  }
 }
 
 // ---- double-float ops (fused FP64 tiles) -----------------------------------------
@@ -837,10 +825,10 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     k_tile(typename GT<T>::G *__restrict__ a, const __grid_constant__ TileArgs p) {
   using C = typename CT<T>::C;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ __align__(8) unsigned long long tc_mbar[kTcMaxBufs];
+  __shared__ __align__(8) unsigned long long tc_mbar[2];
   __shared__ uint32_t tc_tmem_slot;
   __shared__ int tc_abort;
-  TcCtx ctx{0u, 0u, 0u, 1, 0u, 0u};
+  TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1};
   if constexpr (RB < 0) {
     if ((threadIdx.x >> 5) == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -851,9 +839,8 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     }
     if (threadIdx.x == 0) {
       tc_abort = 0;
-      for (int c = 0; c < kTcMaxBufs; ++c)
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[c]))
-                     : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[0])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tc_mbar[1])) : "memory");
       asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
   }
@@ -889,7 +876,8 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     ctx.tmem = tc_tmem_slot;
-    ctx.mbar = smem_u32(&tc_mbar[0]);
+    ctx.mbar[0] = smem_u32(&tc_mbar[0]);
+    ctx.mbar[1] = smem_u32(&tc_mbar[1]);
   }
   constexpr int per16 = 16 / sizeof(C);  // amplitudes per 16-byte chunk
   const unsigned nchunks = (1u << t) / per16;
@@ -965,7 +953,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     if (!ctx.ok) {
       if (threadIdx.x == 0) atomicExch(p.status, 1);
       // let MMAs still in flight finish (bounded) before their TMEM is freed
-      (void)tc_wait(ctx.last_bar, ctx.last_par);
+      (void)tc_wait(ctx.mbar[0], ctx.phase[0]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
