@@ -5,7 +5,7 @@ For a program and a state size it plans and runs every candidate
 the per-pass CUDA events of ``Program.run_profiled``, and keeps the fastest.
 Engines of an FP32 tile: "fma" (every block through shared memory on FP32
 FMAs), "reg" (runs of 1-/2-qubit blocks on amplitudes held in registers) and
-"tc" (blocks merged to 3-4 qubits and run as tcgen05 TF32 MMAs).
+"tc" (blocks merged to 3-5 qubits and run as tcgen05 bf16x3 MMAs).
 Results are cached on the Program object itself, per (qubits, precision,
 candidate list, op-list generation): a freed program's choice can never be
 served to a new one, and adding ops to a program retunes it.
@@ -20,7 +20,8 @@ ENGINES = ("fma", "reg", "tc")
 
 DEFAULT_CANDIDATES = {
     "fp32": [(fw, t, e) for fw in (1, 2) for t in (12, 13, 14) for e in ("fma", "reg")
-             if not (e == "reg" and t == 14)] + [(4, 12, "tc"), (4, 13, "tc"), (2, 13, "tc")],
+             if not (e == "reg" and t == 14)] + [(4, 12, "tc"), (4, 13, "tc"), (5, 13, "tc"),
+                                                   (2, 13, "tc")],
     "fp64": [(fw, t, "fma") for fw in (1, 2, 3) for t in (11, 12, 13)],
 }
 

@@ -413,7 +413,9 @@ static void plan_fused(const std::vector<Op> &ops, int nq, int prec, int fw, int
       }
       flush();
       const bool tc = plan.tensor_cores && prec == QVMG_FP32;
-      if (tc) merge_tile_ops(p, kTcMaxQubits, true);
+      // tensor-core passes merge their dense ops into blocks of up to the
+      // fusion width's qubits (3..5)
+      if (tc) merge_tile_ops(p, std::min(kTcMaxQubits, std::max(kTcMinQubits, fw)), true);
       build_stages(p, prec, plan.reg_stages && !tc);
       return p;
     };

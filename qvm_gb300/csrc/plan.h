@@ -14,7 +14,7 @@ enum OpKind { OP_DENSE = 0, OP_DIAG = 1, OP_PERM = 2, OP_TC = 3 };
 // Tensor-core tile ops: dense blocks of kTcMinQubits..kTcMaxQubits tile
 // bits run as tcgen05 bf16x3 MMAs over chunks of 128 groups.
 constexpr int kTcMinQubits = 3;
-constexpr int kTcMaxQubits = 4;
+constexpr int kTcMaxQubits = 5;
 constexpr int kTcRows = 128;
 
 // One gate application (or fused block).  Qubits are in nat-tuple order:

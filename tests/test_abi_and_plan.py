@@ -95,10 +95,10 @@ def test_fused_plan_equals_circuit(oracle, prec, fw, tile):
             assert st["source_ops"] == len(gs)
 
 
-@pytest.mark.parametrize("fw,tile", [(2, 0), (4, 0), (2, 11), (4, 12), (1, 13)])
+@pytest.mark.parametrize("fw,tile", [(2, 0), (4, 0), (2, 11), (4, 12), (1, 13), (5, 13)])
 def test_tensor_core_plan_equals_circuit(oracle, fw, tile):
-    """FP32 tensor-core planning: the pass-local merge into blocks of <= 4
-    tile bits and the split bf16 operand, executed on the oracle, equal the
+    """FP32 tensor-core planning: the pass-local merge into blocks of up to
+    the fusion width's tile bits (3..5) and the split bf16 operand, executed on the oracle, equal the
     unfused circuit to the hi + lo precision of the block (~2^-17 relative
     per entry)."""
     n = 16
@@ -115,8 +115,8 @@ def test_tensor_core_plan_equals_circuit(oracle, fw, tile):
                if op["kind"] == "tc"]
         if name != "qft":
             assert tcs, name  # the random circuits produce 3-/4-qubit blocks
-        for op in tcs:
-            assert 3 <= len(op["pos"]) <= 4
+        for op in tcs:  # blocks of up to the fusion width's qubits (3..5)
+            assert 3 <= len(op["pos"]) <= min(5, max(3, fw))
         got = run_description(oracle, d, init.copy())
         assert np.max(np.abs(got - want)) < 2e-6, (name, st)
         # FP64 plans never use the tensor cores
