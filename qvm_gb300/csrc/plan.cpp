@@ -420,7 +420,11 @@ static void plan_fused(const std::vector<Op> &ops, int nq, int prec, int fw, int
       return p;
     };
     Pass p = build_pass(in_pass);
-    while (tile_pass_smem_bytes(p, prec) > kTileSmemBudget && in_pass.size() > 1) {
+    // a tensor-core pass keeps two CTAs per SM (one issues MMAs while the
+    // other gathers): its shared memory stays within half an SM's
+    const size_t budget =
+        plan.tensor_cores && prec == QVMG_FP32 ? kTileSmemBudgetTc : kTileSmemBudget;
+    while (tile_pass_smem_bytes(p, prec) > budget && in_pass.size() > 1) {
       remaining.insert(std::lower_bound(remaining.begin(), remaining.end(), in_pass.back()),
                        in_pass.back());
       in_pass.pop_back();

@@ -69,6 +69,9 @@ struct Pass {
 constexpr size_t kTileOpDescBytes = 128;
 constexpr size_t kTileStageDescBytes = 80;
 constexpr size_t kTileSmemBudget = 227 * 1024 - 128;
+// Tensor-core passes: two CTAs per SM share its 228 KiB (each also holding
+// 1 KiB reserved by the runtime and its static variables).
+constexpr size_t kTileSmemBudgetTc = 112 * 1024;
 size_t tile_pass_smem_bytes(const Pass &p, int prec);
 
 // Register bits per thread for a tile of t qubits run by 256 threads:
