@@ -618,15 +618,8 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     for (int s = 0; s < K; ++s) x = inject0u(x, sp[s]);
     return x;
   };
-  // The tile of a tensor-core pass is XOR-swizzled (swz), which is linear
-  // over disjoint bits: a member's address is swz(row part) ^ swz(chunk
-  // part) ^ swz(member offset), with the first and last computed once per op.
-  // The swizzle spreads the lanes of a warp over the banks when a block
-  // holds low tile bits.
-  const unsigned row_base = swz(inject_all((unsigned)(sub * 32 + lane)));
-  auto group_base = [&](unsigned ch) { return row_base ^ swz(inject_all(ch * kTileTcRows)); };
-#pragma unroll
-  for (int i = 0; i < H; ++i) off[i] = swz(off[i]);
+  const unsigned row_base = inject_all((unsigned)(sub * 32 + lane));
+  auto group_base = [&](unsigned ch) { return row_base | inject_all(ch * kTileTcRows); };
   // Chunks go in batches of up to kBufs: the data warps gather and split a
   // whole batch into its TMEM buffers, one barrier hands it to the issuing
   // warp, which issues every chunk's MMAs (each chunk on its own
@@ -641,7 +634,7 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
         const unsigned b = group_base(base + c);
         uint32_t hi[H], lo[H];
 #pragma unroll
-        for (int i = 0; i < H; ++i) bf16_split(tile[b ^ off[i]], hi[i], lo[i]);
+        for (int i = 0; i < H; ++i) bf16_split(tile[b | off[i]], hi[i], lo[i]);
         tmem_st<H>(buf + lanes + kACol + half * H, hi);
         tmem_st<H>(buf + lanes + kACol + D + half * H, lo);
       }
@@ -687,7 +680,7 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
           const unsigned b = group_base(base + c);
 #pragma unroll
           for (int i = 0; i < H; ++i)
-            tile[b ^ off[i]] =
+            tile[b | off[i]] =
                 make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
         }
       }
@@ -932,7 +925,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
       const typename GT<T>::G *src = a + rowoff[el >> L] + (el & rowmask);
-      cp_async16(tile + sw<(RB != 0)>(el), src);
+      cp_async16(tile + sw<(RB > 0)>(el), src);
     }
     cp_async_wait_all();
     if constexpr (kIsDf<T>) {
@@ -965,7 +958,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
           continue;
         }
       }
-      smem_op<T, KMAX, (RB != 0)>(tile, t, L, rowoff, op, data + op.data, p.tables);
+      smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data, p.tables);
       __syncthreads();
     }
     if constexpr (RB < 0) {
@@ -978,7 +971,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
         const double2 v = df_to_double2(tile[el]);
         __stcs(dst, *reinterpret_cast<const int4 *>(&v));
       } else {
-        __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB != 0)>(el)));
+        __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB > 0)>(el)));
       }
     }
   }
