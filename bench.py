@@ -103,9 +103,9 @@ def whole_job_rate(units_per_rank_step: int, steps: int, world: int, max_ms: flo
 
 # DRAM bytes (read + write) of one fused FP32 tile launch at 26 qubits, from
 # the ncu captures summarised under profiles/ (k_tile_fp32_random26_fw2_t13,
-# k_tile_tc_bf16x3_random26_fw4_t13).  Traffic per launch grows with the
+# k_tile_tc_bf16x3_random26_fw5_t13).  Traffic per launch grows with the
 # amplitudes processed, so a launch at n qubits moves 2^(n-26) times as much.
-TILE_TRAFFIC_26Q = {"fma": 536.926208e6 + 475.259648e6, "tc": 536.984064e6 + 475.039744e6}
+TILE_TRAFFIC_26Q = {"fma": 536.926208e6 + 475.259648e6, "tc": 536.99456e6 + 474.37824e6}
 
 
 def traffic_per_launch(n, engine):
