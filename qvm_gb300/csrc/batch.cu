@@ -19,8 +19,9 @@
 // contiguous; then the high qubits with a 2^(26-n)-amplitude row); layer
 // 0's first pass makes its uniform tiles in place instead of reading an
 // initialised state.  (Streaming tiles through two buffers per CTA was
-// measured too: its 128 KiB of buffers leave one CTA per SM, and the
-// 4096-instance batch went from 143 to 199 ms.)  Amplitudes
+// measured too: 13-qubit tiles leave one CTA per SM, 143 -> 199 ms for the
+// 4096-instance batch; 12-qubit tiles keep three CTAs per SM but give
+// 32-byte rows in the second pass at 22 qubits, 140 -> 166 ms.)  Amplitudes
 // are complex FP32; the phase table and RX coefficients are computed in FP64.
 // Each amplitude's cut comes from a per-instance table of the edges inside
 // the low 13 bits, a constant per row for the edges inside the high bits and
