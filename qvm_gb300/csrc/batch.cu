@@ -153,9 +153,8 @@ struct PhaseSrc {
   int ch, m;
   bool split;
   unsigned long long base;  // global index of tile element 0 (edge loop)
-  unsigned jofs;            // low 13 bits of that index (split cut)
   __device__ __forceinline__ float2 at(unsigned j) const {
-    const int cx = split ? cut_split(j | jofs, cl, F, M, ch) : cut_value(base + j, edges, m);
+    const int cx = split ? cut_split(j, cl, F, M, ch) : cut_value(base + j, edges, m);
     return phase[cx];
   }
 };
@@ -312,92 +311,60 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
       const float w = (float)(kform ? rc / rs : rs / rc);
       // a resident state has no cross or high edges: its split cut is cl[x]
       PhaseSrc ph{phase, cl, edges, {0u, 0u, 0u, 0u}, {s_M[0], s_M[1], s_M[2], s_M[3]}, 0, m,
-                  split, 0ull, 0u};
+                  split, 0ull};
       if (resident) {
         tile_rx_run(tile, n, 0, n, w, kform, true, ph);
       } else {
-        // States of <= 24 qubits stream 12-qubit tiles through the two
-        // halves of the tile buffer (the next tile's loads in flight while
-        // the current one is swept); larger ones sweep 13-qubit tiles one at
-        // a time.  Pass A holds tile bits 0..tb-1, pass B the high qubits
-        // tb..n-1 with rows of 2^Lb amplitudes.
-        const bool dbl = n <= 2 * 12;
-        const int tb = dbl ? 12 : kQaoaTileBits;
+        const int tb = kQaoaTileBits;
         const unsigned long long ntiles = len >> tb;
-        auto issue_a = [&](unsigned long long tcount, float2 *dst) {
-          const float4 *src = reinterpret_cast<const float4 *>(psi + (tcount << tb));
-          for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
-            cp_async16(reinterpret_cast<float4 *>(dst) + j, src + j);
-        };
-        // pass A: contiguous tiles, phase + RX on qubits 0..tb-1
+        // pass A: contiguous tiles, phase + RX on qubits 0..12
         for (unsigned long long tcount = 0; tcount < ntiles; ++tcount) {
           const unsigned long long base = tcount << tb;
-          float2 *cur = tile + (dbl ? (unsigned)(tcount & 1) << 12 : 0u);
-          float2 *nxt = tile + ((unsigned)((tcount + 1) & 1) << 12);
-          __syncthreads();  // the previous tile's stores are done with `nxt`
+          __syncthreads();
           if (l == 0) {
             for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              cur[j] = make_float2(amp0, 0.f);
-          } else if (dbl) {
-            if (tcount == 0) {
-              issue_a(0, cur);
-              cp_async_commit();
-            }
-            if (tcount + 1 < ntiles) issue_a(tcount + 1, nxt);
-            cp_async_commit();
-            cp_async_wait_group1();  // tile tcount has landed
+              tile[j] = make_float2(amp0, 0.f);
           } else {
-            issue_a(tcount, cur);
+            // every 16-byte load of the tile in flight at once
+            for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
+              cp_async16(reinterpret_cast<float4 *>(tile) + j,
+                         reinterpret_cast<const float4 *>(psi + base) + j);
             cp_async_wait_all();
           }
-          // the row constants of this tile's 13-bit row, computed by every warp
+          // the row constants of this tile's high part, computed by every warp
           ph.base = base;
-          ph.jofs = (unsigned)(base & ((1u << kQaoaTileBits) - 1u));
-          if (split) cut_row(base >> kQaoaTileBits, edges, s_slot, m, ph.F, ph.ch);
+          if (split) cut_row(tcount, edges, s_slot, m, ph.F, ph.ch);
           __syncthreads();
-          tile_rx_run(cur, tb, 0, tb, w, kform, true, ph);
+          tile_rx_run(tile, tb, 0, tb, w, kform, true, ph);
           for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
-            reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(cur)[j];
+            reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
         }
-        // pass B: rows of 2^Lb amplitudes, the high qubits tb..n-1 in the tile
-        const int hb = n - tb, Lb = tb - hb;  // n <= 2 tb keeps Lb >= 0
-        const bool dblb = dbl && Lb >= 1;
-        auto issue_b = [&](unsigned long long cidx, float2 *dst) {
-          for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
-            unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
-            cp_async16(dst + j, psi + ((h << tb) | (cidx << Lb) | lo));
-          }
-        };
+        // pass B: rows of 2^Lb amplitudes, the high qubits 13..n-1 in the tile
+        const int hb = n - tb, Lb = tb - hb;  // n <= 26 keeps Lb >= 0
         for (unsigned long long cidx = 0; cidx < ntiles; ++cidx) {
-          float2 *cur = tile + (dbl ? (unsigned)(cidx & 1) << 12 : 0u);
-          float2 *nxt = tile + ((unsigned)((cidx + 1) & 1) << 12);
           __syncthreads();
-          if (dblb) {
-            if (cidx == 0) {
-              issue_b(0, cur);
-              cp_async_commit();
+          if (Lb >= 1) {
+            // rows of >= 2 amplitudes: 16-byte asynchronous loads, all in flight
+            for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
+              unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
+              cp_async16(tile + j, psi + ((h << tb) | (cidx << Lb) | lo));
             }
-            if (cidx + 1 < ntiles) issue_b(cidx + 1, nxt);
-            cp_async_commit();
-            cp_async_wait_group1();
-          } else if (Lb >= 1) {
-            issue_b(cidx, cur);
             cp_async_wait_all();
           } else {
             for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              cur[j] = psi[((unsigned long long)j << tb) | cidx];
+              tile[j] = psi[((unsigned long long)j << tb) | cidx];
           }
           __syncthreads();
-          tile_rx_run(cur, tb, Lb, hb, w, kform, false, ph);
+          tile_rx_run(tile, tb, Lb, hb, w, kform, false, ph);
           if (Lb >= 1) {
             for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
               unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
               *reinterpret_cast<float4 *>(psi + ((h << tb) | (cidx << Lb) | lo)) =
-                  *reinterpret_cast<const float4 *>(cur + j);
+                  *reinterpret_cast<const float4 *>(tile + j);
             }
           } else {
             for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              psi[((unsigned long long)j << tb) | cidx] = cur[j];
+              psi[((unsigned long long)j << tb) | cidx] = tile[j];
           }
         }
       }

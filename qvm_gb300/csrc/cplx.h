@@ -253,13 +253,5 @@ __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
-// Close the calling thread's current group of asynchronous copies; wait
-// until at most one of its groups is still pending.
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_group1() {
-  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-}
 
 }  // namespace qvmg
