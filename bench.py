@@ -545,8 +545,8 @@ def run_endpoints(n: int = 26, seed: int = 7):
 def run_random32(fw: int, tile: int, engine: str, shots: int = 4096, seed: int = 3,
                  runs: int = 3, plain: bool = True):
     """The random circuit at 32 qubits (depth 20, 960 gates): fused FP32
-    (32 GiB state) with the tuned engine and with the tensor-core engine;
-    fused FP64 in double-float tiles and the plain FP64 kernels (64 GiB
+    (32 GiB state) with the tuned engine and the other of the FMA and
+    tensor-core engines; fused FP64 in double-float tiles and the plain FP64 kernels (64 GiB
     states each).  Fidelity and max amplitude error of the tuned FP32 state
     against plain FP64, and the shots both draw from the same 4096 uniforms."""
     from qvm_gb300 import CudaPureState, Program, circuits
@@ -556,9 +556,11 @@ def run_random32(fw: int, tile: int, engine: str, shots: int = 4096, seed: int =
     G = len(gates)
     s32 = CudaPureState(n, "fp32")
     out = {"workload": f"random SU(2)/SU(4) circuit, {n} qubits, depth 20, {G} gates"}
-    for label, (f, t, e) in (("fp32_" + engine, (fw, tile, engine)), ("fp32_tc", (4, 13, "tc"))):
-        if label == "fp32_tc" and engine == "tc":
-            continue
+    # the tuned engine, and beside it the other of FMA (fusion width 2) and
+    # tensor cores (fusion width 5)
+    legs = [("fp32_" + engine, (fw, tile, engine))]
+    legs.append(("fp32_fma", (2, 13, "fma")) if engine == "tc" else ("fp32_tc", (5, 13, "tc")))
+    for label, (f, t, e) in legs:
         prog = Program()
         prog.add_gates(gates)
         apply_engine(prog, e)

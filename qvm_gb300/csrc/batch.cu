@@ -14,20 +14,27 @@
 //   <H_C> = sum_x |a_x|^2 cut(x)   (FP64 accumulation)
 //   shots: a two-level CDF (128-amplitude sub-block sums, FP64 prefix)
 //          searched per draw by one warp, smallest x with C(x) >= draw.
-// States of <= 13 qubits live in shared memory for the whole circuit; larger
-// ones stay in HBM and are swept in two tile passes per layer (low 13 qubits
-// contiguous; then the high qubits with a 2^(26-n)-amplitude row); layer
-// 0's first pass makes its uniform tiles in place instead of reading an
-// initialised state.  (Streaming tiles through two buffers per CTA was
-// measured too: 13-qubit tiles leave one CTA per SM, 143 -> 199 ms for the
-// 4096-instance batch; 12-qubit tiles keep three CTAs per SM but give
-// 32-byte rows in the second pass at 22 qubits, 140 -> 166 ms.)  Amplitudes
-// are complex FP32; the phase table and RX coefficients are computed in FP64.
-// Each amplitude's cut comes from a per-instance table of the edges inside
-// the low 13 bits, a constant per row for the edges inside the high bits and
-// popcounts over the cross edges (cut_split).  RX runs in register sweeps
-// of up to four qubits (each thread holds a group of 16 amplitudes), the
-// layer's phase folded into the first sweep.
+// States of <= 13 qubits live in shared memory for the whole circuit.
+// Larger ones stay in HBM and are swept in tile passes of two kinds:
+// contiguous tiles (qubits 0..12) and rows of 2^(26-n) amplitudes holding the
+// high qubits.  The kinds alternate, and each pass finishes the previous
+// layer's RX on the qubits the previous pass lacked, then applies the next
+// layer's phase and its RX on all 13 tile qubits: p layers take p + 1 passes
+// (two per layer before: 4 layers at 22 qubits read and wrote the state 8
+// times, now 5).  The first pass makes its tiles from the uniform state and
+// writes every amplitude's cut value as one byte beside the state; later
+// passes load those bytes with their tiles for the phase, and a last
+// contiguous pass takes <H_C> and the CDF sub-block sums from its tiles.
+// (Streaming tiles through two buffers per CTA was measured too: 13-qubit
+// tiles leave one CTA per SM, 143 -> 199 ms for the 4096-instance batch;
+// 12-qubit tiles keep three CTAs per SM but give 32-byte rows in the second
+// pass at 22 qubits, 140 -> 166 ms.)  Amplitudes are complex FP32; the phase
+// table and RX coefficients are computed in FP64.  The first pass takes each
+// amplitude's cut from a per-instance table of the edges inside the low 13
+// bits, a constant per row for the edges inside the high bits and popcounts
+// over the cross edges (cut_split).  RX runs in register sweeps of up to
+// four qubits (each thread holds a group of 16 amplitudes), a layer's phase
+// folded into the first sweep of its RX.
 // All spin-free: the queue is a plain atomicAdd, no CTA waits on another.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -52,6 +59,7 @@ constexpr int kQaoaSubBits = 7;  // 128-amplitude CDF sub-blocks
 struct QaoaInst {
   unsigned long long state_off;  // float2 offset of the state
   unsigned long long sub_off;    // double offset of the CDF sub-block sums
+  unsigned long long cut_off;    // byte offset of the cut values (states in HBM)
   int n;
   int nedges;
   int edge_off;   // into edges (pairs)
@@ -71,6 +79,7 @@ struct QaoaArgs {
   const double *betas;
   float2 *states;
   double *subs;
+  unsigned char *cuts;        // one cut byte per amplitude of each state in HBM
   const double *draws;        // ninst * nshots, indexed by instance id
   double *expect;             // ninst
   unsigned int *shots;        // ninst * nshots
@@ -143,20 +152,13 @@ __device__ __forceinline__ void rx_pair(float2 &a, float2 &b, float w) {
   }
 }
 
-// Where the layer's phase comes from for an amplitude of a tile: the split
-// cut (low-edge table, row constants F/ch of the tile's high part, slot
-// masks) or the edge loop over the global index.
+// A tile's phases: the layer's table indexed by each amplitude's cut value,
+// held as one byte per tile element (the low-edge table of a resident state,
+// or the cut bytes loaded beside the tile).
 struct PhaseSrc {
   const float2 *phase;
-  const unsigned char *cl, *edges;
-  unsigned F[kCutSlots], M[kCutSlots];
-  int ch, m;
-  bool split;
-  unsigned long long base;  // global index of tile element 0 (edge loop)
-  __device__ __forceinline__ float2 at(unsigned j) const {
-    const int cx = split ? cut_split(j, cl, F, M, ch) : cut_value(base + j, edges, m);
-    return phase[cx];
-  }
+  const unsigned char *cut;
+  __device__ __forceinline__ float2 at(unsigned j) const { return phase[cut[j]]; }
 };
 
 // One register sweep of a shared-memory tile of 2^tb amplitudes: every
@@ -231,12 +233,35 @@ __device__ __forceinline__ double prob_d(float2 v) {
   return (double)v.x * (double)v.x + (double)v.y * (double)v.y;
 }
 
+// RX(2 beta) in the factored form of rx_pair: returns the coefficient w,
+// whether the sine was factored out, and the factor (cos or sin beta).
+__device__ __forceinline__ float rx_coef(double beta, bool &kform, double &factor) {
+  double rs, rc;
+  sincos(beta, &rs, &rc);
+  kform = fabs(rs) > fabs(rc);
+  factor = kform ? rs : rc;
+  return (float)(kform ? rc / rs : rs / rc);
+}
+
+// A layer's phase table exp(-i gamma (m - 2c) / 2), c = 0..m, scaled by the
+// RX factor of all n qubits (rx_coef); the CTA's threads share the entries.
+__device__ __forceinline__ void phase_table(float2 *phase, double gamma, double factor, int n,
+                                            int m) {
+  const double fac = pow(factor, (double)n);
+  for (int c = threadIdx.x; c <= m; c += blockDim.x) {
+    double sn, cs;
+    sincos(-gamma * (double)(m - 2 * c) * 0.5, &sn, &cs);
+    phase[c] = make_float2((float)(fac * cs), (float)(fac * sn));
+  }
+}
+
 __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_constant__ QaoaArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *tile = reinterpret_cast<float2 *>(smem);                     // 2^13
-  float2 *phase = tile + (1u << kQaoaTileBits);                         // kQaoaMaxEdges+1
+  // 2^13 cut bytes (the low-edge table, or a tile's cut values), 16-byte aligned
+  unsigned char *cl = smem + (8u << kQaoaTileBits);
+  float2 *phase = reinterpret_cast<float2 *>(cl + (1u << kQaoaTileBits));  // kQaoaMaxEdges+1
   unsigned char *edges = reinterpret_cast<unsigned char *>(phase + kQaoaMaxEdges + 1);
-  unsigned char *cl = edges + 2 * kQaoaMaxEdges;                        // 2^13 low-edge cuts
   __shared__ double red[kQaoaThreads / 32];
   __shared__ int s_inst;
   __shared__ unsigned char s_slot[kQaoaMaxEdges];
@@ -289,76 +314,139 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
     const unsigned long long len = 1ull << n;
     const float amp0 = (float)(1.0 / sqrt((double)len));
     const bool resident = n <= kQaoaTileBits;
-    // H on all qubits: a resident state starts in the tile; a state in HBM
-    // is never written uniform -- layer 0's first pass makes its tiles
-    if (resident)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int sbits = n < kQaoaSubBits ? n : kQaoaSubBits;
+    const unsigned long long nsub = len >> sbits;
+    double *sub = A.subs + I.sub_off;
+    // every amplitude's cut value: the low-edge table of a resident state,
+    // the bytes beside a state in HBM
+    unsigned char *cuts = resident ? cl : A.cuts + I.cut_off;
+    double ex = 0.0;      // this lane's share of <H_C>
+    bool summed = false;  // sub-block sums and <H_C> taken in the last tile pass
+    const PhaseSrc ph{phase, cl};
+    if (resident) {
+      // H on all qubits, then every layer on the state held in the tile
       for (unsigned x = threadIdx.x; x < len; x += blockDim.x) tile[x] = make_float2(amp0, 0.f);
-    for (int l = 0; l < A.p; ++l) {
-      const double g = A.gammas[I.param_off + l], b = A.betas[I.param_off + l];
-      __syncthreads();
-      // RX(2 beta) with its larger coefficient factored out (rx_pair); the
-      // factor for all n qubits scales the layer's phase table
-      double rs, rc;
-      sincos(b, &rs, &rc);
-      const bool kform = fabs(rs) > fabs(rc);
-      const double fac = pow(kform ? rs : rc, (double)n);
-      for (int c = threadIdx.x; c <= m; c += blockDim.x) {
-        double sn, cs;
-        sincos(-g * (double)(m - 2 * c) * 0.5, &sn, &cs);
-        phase[c] = make_float2((float)(fac * cs), (float)(fac * sn));
+      for (int l = 0; l < A.p; ++l) {
+        __syncthreads();
+        bool kf;
+        double f1;
+        const float w = rx_coef(A.betas[I.param_off + l], kf, f1);
+        phase_table(phase, A.gammas[I.param_off + l], f1, n, m);
+        __syncthreads();
+        tile_rx_run(tile, n, 0, n, w, kf, true, ph);
       }
       __syncthreads();
-      const float w = (float)(kform ? rc / rs : rs / rc);
-      // a resident state has no cross or high edges: its split cut is cl[x]
-      PhaseSrc ph{phase, cl, edges, {0u, 0u, 0u, 0u}, {s_M[0], s_M[1], s_M[2], s_M[3]}, 0, m,
-                  split, 0ull};
-      if (resident) {
-        tile_rx_run(tile, n, 0, n, w, kform, true, ph);
-      } else {
-        const int tb = kQaoaTileBits;
-        const unsigned long long ntiles = len >> tb;
-        // pass A: contiguous tiles, phase + RX on qubits 0..12
-        for (unsigned long long tcount = 0; tcount < ntiles; ++tcount) {
-          const unsigned long long base = tcount << tb;
+      for (unsigned x = threadIdx.x; x < len; x += blockDim.x) psi[x] = tile[x];
+      __syncthreads();
+    } else {
+      // Tile passes over the state in HBM.  Type A passes (even) take
+      // contiguous tiles, qubits 0..12; type B passes (odd) take rows of
+      // 2^Lb amplitudes, qubits 0..Lb-1 and the high qubits 13..n-1.  Pass i
+      // finishes layer i-1's RX on the tile bits Lb..12 (the qubits the
+      // previous pass lacked), then applies layer i's phase and its RX on all
+      // 13 tile qubits: p layers take p + 1 passes.  Pass 0 makes its tiles
+      // from the uniform state and writes each amplitude's cut value (one
+      // byte) beside the state; later passes load those bytes with the tile,
+      // into the low-edge table's space.
+      const int tb = kQaoaTileBits, hb = n - tb, Lb = tb - hb;  // n <= 26 keeps Lb >= 0
+      const unsigned long long ntiles = len >> tb;
+      const unsigned lomask = (1u << Lb) - 1u;
+      const unsigned M[kCutSlots] = {s_M[0], s_M[1], s_M[2], s_M[3]};
+      bool kf_prev = false;
+      float w_prev = 0.f;
+      for (int pass = 0; pass <= A.p; ++pass) {
+        const bool rows = (pass & 1) != 0;
+        const bool last = pass == A.p;
+        bool kf = false;
+        float w = 0.f;
+        __syncthreads();  // the previous pass's phase table is no longer read
+        if (!last) {
+          double f1;
+          w = rx_coef(A.betas[I.param_off + pass], kf, f1);
+          phase_table(phase, A.gammas[I.param_off + pass], f1, n, m);
+        }
+        for (unsigned long long cidx = 0; cidx < ntiles; ++cidx) {
           __syncthreads();
-          if (l == 0) {
-            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              tile[j] = make_float2(amp0, 0.f);
-          } else {
-            // every 16-byte load of the tile in flight at once
+          if (pass == 0) {
+            // uniform amplitudes times layer 0's phase; the cut bytes go out
+            const unsigned long long base = cidx << tb;
+            unsigned F[kCutSlots] = {0u, 0u, 0u, 0u};
+            int ch = 0;
+            if (split) cut_row(cidx, edges, s_slot, m, F, ch);
+            for (unsigned q = threadIdx.x; q < (1u << tb) / 4; q += blockDim.x) {
+              unsigned word = 0;
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const unsigned j = 4 * q + e;
+                const int cx = split ? cut_split(j, cl, F, M, ch) : cut_value(base + j, edges, m);
+                const float2 f = phase[cx];
+                tile[j] = make_float2(amp0 * f.x, amp0 * f.y);
+                word |= (unsigned)cx << (8 * e);
+              }
+              reinterpret_cast<unsigned *>(cuts + base)[q] = word;
+            }
+          } else if (!rows) {
+            // every 16-byte load of the tile and its cut bytes in flight at once
+            const unsigned long long base = cidx << tb;
             for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
               cp_async16(reinterpret_cast<float4 *>(tile) + j,
                          reinterpret_cast<const float4 *>(psi + base) + j);
-            cp_async_wait_all();
-          }
-          // the row constants of this tile's high part, computed by every warp
-          ph.base = base;
-          if (split) cut_row(tcount, edges, s_slot, m, ph.F, ph.ch);
-          __syncthreads();
-          tile_rx_run(tile, tb, 0, tb, w, kform, true, ph);
-          for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
-            reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
-        }
-        // pass B: rows of 2^Lb amplitudes, the high qubits 13..n-1 in the tile
-        const int hb = n - tb, Lb = tb - hb;  // n <= 26 keeps Lb >= 0
-        for (unsigned long long cidx = 0; cidx < ntiles; ++cidx) {
-          __syncthreads();
-          if (Lb >= 1) {
-            // rows of >= 2 amplitudes: 16-byte asynchronous loads, all in flight
-            for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
-              unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
-              cp_async16(tile + j, psi + ((h << tb) | (cidx << Lb) | lo));
-            }
+            for (unsigned j = threadIdx.x; j < (1u << tb) / 16; j += blockDim.x)
+              cp_async16(cl + 16 * j, cuts + base + 16 * j);
             cp_async_wait_all();
           } else {
-            for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
-              tile[j] = psi[((unsigned long long)j << tb) | cidx];
+            if (Lb >= 1) {
+              // rows of >= 2 amplitudes: 16-byte asynchronous loads
+              for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
+                const unsigned long long h = j >> Lb, lo = j & lomask;
+                cp_async16(tile + j, psi + ((h << tb) | (cidx << Lb) | lo));
+              }
+            } else {
+              for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x)
+                tile[j] = psi[((unsigned long long)j << tb) | cidx];
+            }
+            if (Lb >= 4) {
+              for (unsigned j = 16 * threadIdx.x; j < (1u << tb); j += 16 * blockDim.x) {
+                const unsigned long long h = j >> Lb, lo = j & lomask;
+                cp_async16(cl + j, cuts + ((h << tb) | (cidx << Lb) | lo));
+              }
+            } else {
+              for (unsigned j = threadIdx.x; j < (1u << tb); j += blockDim.x) {
+                const unsigned long long h = j >> Lb, lo = j & lomask;
+                cl[j] = cuts[(h << tb) | (cidx << Lb) | lo];
+              }
+            }
+            cp_async_wait_all();
           }
           __syncthreads();
-          tile_rx_run(tile, tb, Lb, hb, w, kform, false, ph);
-          if (Lb >= 1) {
+          if (pass > 0) tile_rx_run(tile, tb, Lb, hb, w_prev, kf_prev, false, ph);
+          if (!last) {
+            tile_rx_run(tile, tb, 0, tb, w, kf, pass > 0, ph);
+          } else if (!rows) {
+            // the last pass holds contiguous tiles: their 128-amplitude
+            // sub-block sums and <H_C> terms, one warp per sub-block
+            const unsigned long long s0 = cidx << (tb - kQaoaSubBits);
+            for (unsigned sb = warp; sb < (1u << (tb - kQaoaSubBits)); sb += nwarps) {
+              float hi = 0.f, lo = 0.f, exf = 0.f;
+              for (unsigned j = lane; j < (1u << kQaoaSubBits); j += 32) {
+                const unsigned t = (sb << kQaoaSubBits) + j;
+                const float2 v = tile[t];
+                df_add_prob(hi, lo, v);  // exact squares for the CDF
+                exf = fmaf(fmaf(v.x, v.x, v.y * v.y), (float)cl[t], exf);
+              }
+              const double acc = warp_sum_d((double)hi + (double)lo);
+              ex += (double)exf;
+              if (lane == 0) sub[s0 + sb] = acc;
+            }
+          }
+          if (!rows) {
+            const unsigned long long base = cidx << tb;
+            for (unsigned j = threadIdx.x; j < (1u << tb) / 2; j += blockDim.x)
+              reinterpret_cast<float4 *>(psi + base)[j] = reinterpret_cast<const float4 *>(tile)[j];
+          } else if (Lb >= 1) {
             for (unsigned j = 2 * threadIdx.x; j < (1u << tb); j += 2 * blockDim.x) {
-              unsigned long long h = j >> Lb, lo = j & ((1u << Lb) - 1u);
+              const unsigned long long h = j >> Lb, lo = j & lomask;
               *reinterpret_cast<float4 *>(psi + ((h << tb) | (cidx << Lb) | lo)) =
                   *reinterpret_cast<const float4 *>(tile + j);
             }
@@ -367,38 +455,26 @@ __global__ void __launch_bounds__(kQaoaThreads, 3) k_qaoa_batch(const __grid_con
               psi[((unsigned long long)j << tb) | cidx] = tile[j];
           }
         }
+        w_prev = w;
+        kf_prev = kf;
       }
-    }
-    __syncthreads();
-    if (resident) {
-      for (unsigned x = threadIdx.x; x < len; x += blockDim.x) psi[x] = tile[x];
+      summed = (A.p & 1) == 0;
       __syncthreads();
     }
-    // expectation and 128-amplitude sub-block sums (one warp per sub-block)
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int sbits = n < kQaoaSubBits ? n : kQaoaSubBits;
-    const unsigned long long nsub = len >> sbits;
-    double *sub = A.subs + I.sub_off;
-    double ex = 0.0;
-    const unsigned M[kCutSlots] = {s_M[0], s_M[1], s_M[2], s_M[3]};
-    for (unsigned long long sb = warp; sb < nsub; sb += nwarps) {
-      float hi = 0.f, lo = 0.f, exf = 0.f;
-      unsigned F[kCutSlots] = {0u, 0u, 0u, 0u};
-      int ch = 0;
-      // a sub-block (2^7 amplitudes) lies within one 2^13 row: one high part
-      if (split && !resident) cut_row((sb << sbits) >> kQaoaTileBits, edges, s_slot, m, F, ch);
-      for (unsigned j = lane; j < (1u << sbits); j += 32) {
-        unsigned long long x = (sb << sbits) + j;
-        float2 v = psi[x];
-        df_add_prob(hi, lo, v);  // exact squares for the CDF
-        const int cx = !split ? cut_value(x, edges, m)
-                       : resident ? (int)cl[x]
-                                  : cut_split((unsigned)(x & ((1u << kQaoaTileBits) - 1u)), cl, F, M, ch);
-        exf = fmaf(fmaf(v.x, v.x, v.y * v.y), (float)cx, exf);
+    if (!summed) {
+      // expectation and 128-amplitude sub-block sums (one warp per sub-block)
+      for (unsigned long long sb = warp; sb < nsub; sb += nwarps) {
+        float hi = 0.f, lo = 0.f, exf = 0.f;
+        for (unsigned j = lane; j < (1u << sbits); j += 32) {
+          const unsigned long long x = (sb << sbits) + j;
+          const float2 v = psi[x];
+          df_add_prob(hi, lo, v);  // exact squares for the CDF
+          exf = fmaf(fmaf(v.x, v.x, v.y * v.y), (float)cuts[x], exf);
+        }
+        const double acc = warp_sum_d((double)hi + (double)lo);
+        ex += (double)exf;
+        if (lane == 0) sub[sb] = acc;
       }
-      double acc = warp_sum_d((double)hi + (double)lo);
-      ex += (double)exf;
-      if (lane == 0) sub[sb] = acc;
     }
     ex = warp_sum_d(ex);
     if (lane == 0) red[warp] = ex;
@@ -480,6 +556,7 @@ struct qvmg_qaoa_s {
   void *dbuf = nullptr;              // instances, edges, params
   float2 *states = nullptr;
   double *subs = nullptr;
+  unsigned char *cuts = nullptr;
   double *draws = nullptr;
   double *expect = nullptr;
   unsigned int *shots = nullptr;
@@ -500,6 +577,7 @@ static void qaoa_release(qvmg_qaoa_batch b) {
   cudaFree(b->dbuf);
   cudaFree(b->states);
   cudaFree(b->subs);
+  cudaFree(b->cuts);
   cudaFree(b->draws);
   cudaFree(b->expect);
   cudaFree(b->shots);
@@ -520,7 +598,7 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
   if (p < 1 || p > kQaoaMaxLayers) return fail(QVMG_E_INVALID, "QAOA depth must be 1..16");
   std::vector<QaoaInst> inst(ninst);
   std::vector<unsigned char> e8;
-  unsigned long long soff = 0, uoff = 0;
+  unsigned long long soff = 0, uoff = 0, coff = 0;
   int eoff = 0;
   for (int i = 0; i < ninst; ++i) {
     int n = nqubits[i];
@@ -556,6 +634,8 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
     QaoaInst q = inst[order[r]];
     q.state_off = soff;
     q.sub_off = uoff;
+    q.cut_off = coff;  // multiples of 2^14: 16-byte aligned
+    if (q.n > kQaoaTileBits) coff += 1ull << q.n;
     b->state_off[q.id] = soff;
     soff += 1ull << q.n;
     int sb = q.n < kQaoaSubBits ? q.n : kQaoaSubBits;
@@ -586,10 +666,11 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
   QCHK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
   QCHK(cudaMalloc(&b->states, soff * sizeof(float2)), "cudaMalloc(batch states)");
   QCHK(cudaMalloc(&b->subs, uoff * sizeof(double)), "cudaMalloc(batch CDF)");
+  QCHK(cudaMalloc(&b->cuts, coff ? coff : 16), "cudaMalloc(batch cut values)");
   QCHK(cudaMalloc(&b->expect, ninst * sizeof(double)), "cudaMalloc(expectations)");
   QCHK(cudaMalloc(&b->counter, sizeof(unsigned int)), "cudaMalloc(counter)");
 #undef QCHK
-  b->bytes = host.size() + soff * sizeof(float2) + uoff * sizeof(double) + ninst * 8;
+  b->bytes = host.size() + soff * sizeof(float2) + uoff * sizeof(double) + coff + ninst * 8;
   QaoaArgs &A = b->args;
   A.ninst = ninst;
   A.p = p;
@@ -599,6 +680,7 @@ int qvmg_qaoa_batch_create(int ninst, const int *nqubits, const int *nedges, con
   A.betas = (const double *)((unsigned char *)b->dbuf + ib + eb + pb);
   A.states = b->states;
   A.subs = b->subs;
+  A.cuts = b->cuts;
   A.expect = b->expect;
   A.counter = b->counter;
   static std::once_flag attr_once;

@@ -307,8 +307,10 @@ class Program:
         L.call("qvmg_program_set_option", self._h, 1, 1 if enable else 0)
 
     def set_tensor_cores(self, enable: bool):
-        """Merge the dense blocks of FP32 tiles into blocks of up to 4 qubits
-        and run the 3- and 4-qubit ones on the tensor cores."""
+        """Merge the dense blocks of FP32 tiles into blocks of up to
+        min(5, max(3, fusion_width)) qubits and run the 3- to 5-qubit ones as
+        tcgen05 MMAs in bf16x3 split precision (three bf16 products per
+        FP32 product, FP32 accumulation)."""
         L.call("qvmg_program_set_option", self._h, 2, 1 if enable else 0)
 
     def num_ops(self) -> int:

@@ -139,3 +139,43 @@ def test_qaoa_batch_shot_buffer_failure_leaves_batch_usable(gpu):
     np.testing.assert_array_equal(s64, fs64)
     b.free()
     fresh.free()
+
+
+def test_qaoa_batch_wide_instances_match_oracle(gpu, oracle):
+    """Instances of 23-26 qubits, whose row passes hold rows of 8, 2, 4 and
+    1 amplitudes (their cut bytes then load one by one): depth 1 ends on a
+    row pass, so <H_C> and the CDF are read back from HBM; depth 2 ends on a
+    contiguous pass, which sums them from its tiles.  Against the oracle:
+    amplitudes, <H_C> and 256 shots per instance."""
+    oracle.set_workers(os.cpu_count() or 1)
+    rng = np.random.default_rng(21)
+
+    def ring_with_chords(n, chords):
+        e = [(i, (i + 1) % n) for i in range(n)]
+        while len(e) < n + chords:
+            u, v = (int(x) for x in rng.choice(n, 2, replace=False))
+            if (u, v) not in e and (v, u) not in e:
+                e.append((u, v))
+        return e
+
+    cases = ((1, [(23, ring_with_chords(23, 10)), (26, circuits.random_3_regular_graph(26, rng))]),
+             (2, [(24, circuits.random_3_regular_graph(24, rng)), (25, ring_with_chords(25, 8))]))
+    for p, graphs in cases:
+        gam = rng.uniform(0, np.pi, (len(graphs), p))
+        bet = rng.uniform(0, np.pi / 2, (len(graphs), p))
+        b = QaoaBatch(graphs, gam, bet)
+        draws = np.random.default_rng(22).random((len(graphs), 256))
+        ex, shots = b.run(draws)
+        for i, (n, edges) in enumerate(graphs):
+            want = oracle_qaoa(oracle, n, edges, gam[i], bet[i])
+            got = b.state(i)
+            assert np.max(np.abs(got - want)) < 2e-6, (p, n)
+            wex = float(np.sum(np.abs(want) ** 2 * circuits.maxcut_values(n, edges)))
+            assert abs(ex[i] - wex) < 1e-5 * max(1.0, wex), (p, n, ex[i], wex)
+            ref = got.astype(np.complex64).astype(np.complex128)
+            tot = np.sum(np.abs(ref) ** 2)
+            wsh = oracle.sample_multiple(ref, draws[i] * tot)
+            cdf = np.cumsum(np.abs(ref) ** 2)
+            near = np.array([np.min(np.abs(cdf - d * tot)) < 1e-9 for d in draws[i]])
+            assert ((shots[i] == wsh) | near).all(), (p, n)
+        b.free()
