@@ -358,12 +358,12 @@ def run_plain_passes(runs: int = 5, seed: int = 9):
 
 
 def run_engines_other(runs: int = 2):
-    """The FP32 tile engines on circuits other than the headline: the
-    config-1 family (H, then RX/RZ on every qubit and CNOTs on alternating
-    pairs per layer) at 28 qubits with 10 layers, and the QFT at 30 qubits.
-    Each runs fused with the FMA engine (fusion width 2, 13-qubit tiles) and
-    with the tensor-core engine (fusion width 4, 12-qubit tiles); device ms
-    per run from per-pass events, plus the plan's tensor-core block count."""
+    """The FP32 tile engines on circuits other than the headline: the layer
+    circuit (H, then RX/RZ on every qubit and CNOTs on alternating pairs per
+    layer) at 28 qubits with 10 layers, and the QFT at 30 qubits.  Each runs
+    fused with the FMA engine (fusion width 2, 13-qubit tiles) and with the
+    tensor-core engine (fusion width 5, 13-qubit tiles); device ms per run
+    from per-pass events, plus the plan's tensor-core block count."""
     from qvm_gb300 import CudaPureState, Program, circuits
     from qvm_gb300.autotune import apply_engine
     out = {}
@@ -371,7 +371,7 @@ def run_engines_other(runs: int = 2):
                            ("qft30", 30, circuits.qft(30))):
         s = CudaPureState(n, "fp32")
         row = {"qubits": n, "gates": len(gates)}
-        for engine, fw, tile in (("fma", 2, 13), ("tc", 4, 12)):
+        for engine, fw, tile in (("fma", 2, 13), ("tc", 5, 13)):
             p = Program()
             p.add_gates(gates)
             apply_engine(p, engine)
