@@ -59,6 +59,15 @@ __device__ __forceinline__ unsigned inject0u(unsigned x, int q) {
 
 // ---- shared-memory ops -----------------------------------------------------------
 
+// The threads that work on one tile (a tile CTA): the ops take their thread
+// index, count and barrier from here rather than from the launch shape.
+struct Team {
+  unsigned id;        // thread index within the team
+  unsigned n;         // threads in the team
+  unsigned warp_sub;  // this warp's quarter of TMEM lanes (CTA warp index % 4)
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+
 // FP32 1-/2-qubit block with 16-byte shared-memory accesses.  Tile bit 0
 // pairs two amplitudes in one 16-byte word: if it is a target, a group's
 // amplitudes c and c | b0 come in one load; otherwise each thread takes the
@@ -69,14 +78,14 @@ __device__ __forceinline__ unsigned inject0u(unsigned x, int q) {
 // unfused.
 template <int K, int J0>
 __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 *m,
-                                              const unsigned *off, const int *sp) {
+                                              const unsigned *off, const int *sp, const Team &tm) {
   constexpr int D = 1 << K;
   float4 *t4 = reinterpret_cast<float4 *>(tile);
   if constexpr (J0 >= 0) {
     // the target on tile bit 0 is matrix bit J0: amplitudes c and c | (1 << J0)
     // share a 16-byte word.  sp[0] == 0; inject the other targets.
     const unsigned ngroups = 1u << (t - K);
-    for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
+    for (unsigned g = tm.id; g < ngroups; g += tm.n) {
       unsigned b = g << 1;
 #pragma unroll
       for (int s = 1; s < K; ++s) b = inject0u(b, sp[s]);
@@ -106,7 +115,7 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
   } else {
     // no target on bit 0: the groups at b and b | 1 share every 16-byte word
     const unsigned npairs = 1u << (t - K - 1);
-    for (unsigned g = threadIdx.x; g < npairs; g += blockDim.x) {
+    for (unsigned g = tm.id; g < npairs; g += tm.n) {
       unsigned b = g << 1;
 #pragma unroll
       for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
@@ -133,7 +142,7 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
 
 template <typename T, int K, bool S>
 __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const TileOpDev &op,
-                                           const typename CT<T>::C *mat) {
+                                           const typename CT<T>::C *mat, const Team &tm) {
   using C = typename CT<T>::C;
   constexpr int D = 1 << K;
   int sp[K];
@@ -169,13 +178,13 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
     for (int i = 0; i < D * D; ++i) mreg[i] = mat[i];
   }
   if constexpr (std::is_same<T, float>::value && !S && K <= 2) {
-    if (op.pos[0] == 0) tile_dense_v4<K, 0>(tile, t, mreg, off, sp);
-    else if (K == 2 && op.pos[K - 1] == 0) tile_dense_v4<K, K - 1>(tile, t, mreg, off, sp);
-    else tile_dense_v4<K, -1>(tile, t, mreg, off, sp);
+    if (op.pos[0] == 0) tile_dense_v4<K, 0>(tile, t, mreg, off, sp, tm);
+    else if (K == 2 && op.pos[K - 1] == 0) tile_dense_v4<K, K - 1>(tile, t, mreg, off, sp, tm);
+    else tile_dense_v4<K, -1>(tile, t, mreg, off, sp, tm);
     return;
   }
   const unsigned ngroups = 1u << (t - K);
-  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
+  for (unsigned g = tm.id; g < ngroups; g += tm.n) {
     unsigned b = g;
 #pragma unroll
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
@@ -196,7 +205,8 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
 }
 
 template <typename T, int K, bool S>
-__device__ __forceinline__ void tile_perm(typename CT<T>::C *tile, int t, const TileOpDev &op) {
+__device__ __forceinline__ void tile_perm(typename CT<T>::C *tile, int t, const TileOpDev &op,
+                                          const Team &tm) {
   using C = typename CT<T>::C;
   constexpr int D = 1 << K;
   int sp[K];
@@ -222,7 +232,7 @@ __device__ __forceinline__ void tile_perm(typename CT<T>::C *tile, int t, const 
   }
   const int nm = op.nmoved;
   const unsigned ngroups = 1u << (t - K);
-  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
+  for (unsigned g = tm.id; g < ngroups; g += tm.n) {
     unsigned b = g;
 #pragma unroll
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
@@ -273,18 +283,25 @@ __device__ __forceinline__ unsigned diag_tile_element(const TileDiagInfo &di, un
 }
 
 // Whether a thread's table index is the same for all its elements.  Thread
-// x takes elements u = x + k * blockDim (count and blockDim powers of two);
+// x takes elements u = x + k * nthreads (count and nthreads powers of two);
 // inserting the required bits is linear over disjoint bits, so its elements
-// differ only in the tile bits that the u bits at and above log2(blockDim)
+// differ only in the tile bits that the u bits at and above log2(nthreads)
 // land on.  If the table holds none of those bits, one lookup serves them all.
 __device__ __forceinline__ bool diag_thread_constant(const TileDiagInfo &di, const TileOpDev &op,
-                                                     unsigned count) {
-  const unsigned uvary = (count - 1u) & ~(blockDim.x - 1u);
+                                                     unsigned count, unsigned nthreads) {
+  const unsigned uvary = (count - 1u) & ~(nthreads - 1u);
   const unsigned vmask = diag_tile_element(di, uvary) & ~diag_tile_element(di, 0u);
   unsigned tmask = 0;
   for (int i = 0; i < op.k; ++i)
     if (di.tpos[i] != 255) tmask |= 1u << di.tpos[i];
   return (tmask & vmask) == 0;
+}
+
+// The threads of a team that take part in a diagonal op: the largest power
+// of two not above the team's size (the thread-constant test above needs a
+// power-of-two stride; tensor-core CTAs have 288 threads).
+__device__ __forceinline__ unsigned diag_threads(const Team &tm) {
+  return 1u << (31 - __clz(tm.n));
 }
 
 // Diagonal op: each element's table entry multiplies it (entries of 1 are
@@ -296,23 +313,24 @@ __device__ __forceinline__ bool diag_thread_constant(const TileDiagInfo &di, con
 template <typename T, bool S>
 __device__ __forceinline__ void tile_diag(typename CT<T>::C *tile, int t, int L,
                                           const unsigned long long *rowoff, const TileOpDev &op,
-                                          const typename CT<T>::C *table) {
+                                          const typename CT<T>::C *table, const Team &tm) {
   using C = typename CT<T>::C;
   const TileDiagInfo &di = *reinterpret_cast<const TileDiagInfo *>(op.src);
   const int cidx = diag_tile_const(di, op, rowoff);
   if (cidx < 0) return;
   const unsigned count = (1u << t) >> di.nreq;
-  if (threadIdx.x >= count) return;
-  if (diag_thread_constant(di, op, count)) {
-    const C ph = __ldg(table + diag_tile_index(di, op, cidx, diag_tile_element(di, threadIdx.x)));
+  const unsigned nt = diag_threads(tm);
+  if (tm.id >= count || tm.id >= nt) return;
+  if (diag_thread_constant(di, op, count, nt)) {
+    const C ph = __ldg(table + diag_tile_index(di, op, cidx, diag_tile_element(di, tm.id)));
     if (ph.x == (T)1 && ph.y == (T)0) return;
-    for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+    for (unsigned u = tm.id; u < count; u += nt) {
       const unsigned p = sw<S>(diag_tile_element(di, u));
       tile[p] = cmul(tile[p], ph);
     }
     return;
   }
-  for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+  for (unsigned u = tm.id; u < count; u += nt) {
     const unsigned j = diag_tile_element(di, u);
     const C ph = __ldg(table + diag_tile_index(di, op, cidx, j));
     if (ph.x != (T)1 || ph.y != (T)0) {
@@ -573,16 +591,17 @@ __device__ __forceinline__ void bf16_split(float2 v, uint32_t &hi, uint32_t &lo)
 template <int K>
 __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op,
                                         const unsigned char *bmat, TcCtx &ctx,
-                                        volatile int *abort_flag) {
+                                        volatile int *abort_flag, const Team &tm) {
   constexpr int D = 1 << K, NC = 2 * D, H = D / 2;
   constexpr uint32_t kSboB = 2 * 16 * D;   // Bt rows hold 2D bf16 (4D bytes); 8 rows per group
   constexpr uint32_t kPieceB = 8 * D * D;  // bytes of Bt hi (then Bt lo)
   constexpr int kSteps = NC / 16;          // 16-element K steps per piece (8 TMEM columns)
   constexpr int kBufCols = 4 * D, kACol = 2 * D;  // per chunk: D | A hi | A lo
   constexpr unsigned kBufs = kTcCols / kBufCols;  // chunks per batch
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = (int)(tm.id >> 5), lane = (int)(tm.id & 31);
   const bool issuer = warp == kTileThreads / 32;  // the extra warp issues the MMAs
-  const int sub = warp & 3, half = (warp >> 2) & 1;
+  // a warp reaches the TMEM lanes of its quarter: CTA warp index mod 4
+  const int sub = (int)tm.warp_sub, half = (warp >> 2) & 1;
   int sp[K];
 #pragma unroll
   for (int i = 0; i < K; ++i) sp[i] = op.pos[i];
@@ -641,7 +660,7 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
       asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
+    tm.sync();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (*abort_flag) {  // uniform: read after the barrier
       ctx.ok = 0;
@@ -687,7 +706,7 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     }
     ctx.phase[0] ^= 1u;  // every thread: the barrier's next phase
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();  // the batch's buffers are read out before the next one is written
+    tm.sync();  // the batch's buffers are read out before the next one is written
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   }
   if (*abort_flag) {  // a wait that gave up on the last batch (seen after its barrier)
@@ -712,7 +731,7 @@ template <typename T>
 constexpr bool kIsDf = std::is_same<T, dfloat>::value;
 
 template <int K, bool S>
-__device__ __forceinline__ void tile_dense_df(dfc *tile, int t, const TileOpDev &op,
+__device__ __forceinline__ void tile_dense_df(dfc *tile, int t, const Team &tm, const TileOpDev &op,
                                               const dfc *mat) {
   constexpr int D = 1 << K;
   int sp[K];
@@ -743,7 +762,7 @@ __device__ __forceinline__ void tile_dense_df(dfc *tile, int t, const TileOpDev 
     for (int i = 0; i < D * D; ++i) mreg[i] = mat[i];
   }
   const unsigned ngroups = 1u << (t - K);
-  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x) {
+  for (unsigned g = tm.id; g < ngroups; g += tm.n) {
     unsigned b = g;
 #pragma unroll
     for (int s = 0; s < K; ++s) b = inject0u(b, sp[s]);
@@ -766,24 +785,25 @@ __device__ __forceinline__ void tile_dense_df(dfc *tile, int t, const TileOpDev 
 template <bool S>
 __device__ __forceinline__ void tile_diag_df(dfc *tile, int t, int L,
                                              const unsigned long long *rowoff, const TileOpDev &op,
-                                             const dfc *table) {
+                                             const dfc *table, const Team &tm) {
   const TileDiagInfo &di = *reinterpret_cast<const TileDiagInfo *>(op.src);
   const int cidx = diag_tile_const(di, op, rowoff);
   if (cidx < 0) return;
   const unsigned count = (1u << t) >> di.nreq;
-  if (threadIdx.x >= count) return;
-  if (diag_thread_constant(di, op, count)) {
+  const unsigned nt = diag_threads(tm);
+  if (tm.id >= count || tm.id >= nt) return;
+  if (diag_thread_constant(di, op, count, nt)) {
     const float4 e = __ldg(reinterpret_cast<const float4 *>(table) +
-                           diag_tile_index(di, op, cidx, diag_tile_element(di, threadIdx.x)));
+                           diag_tile_index(di, op, cidx, diag_tile_element(di, tm.id)));
     if (e.x == 1.f && e.y == 0.f && e.z == 0.f && e.w == 0.f) return;
     const dfc ph{e.x, e.y, e.z, e.w};
-    for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+    for (unsigned u = tm.id; u < count; u += nt) {
       const unsigned p = sw<S>(diag_tile_element(di, u));
       tile[p] = df_cmul(tile[p], ph);
     }
     return;
   }
-  for (unsigned u = threadIdx.x; u < count; u += blockDim.x) {
+  for (unsigned u = tm.id; u < count; u += nt) {
     const unsigned j = diag_tile_element(di, u);
     const float4 e =
         __ldg(reinterpret_cast<const float4 *>(table) + diag_tile_index(di, op, cidx, j));
@@ -796,53 +816,76 @@ __device__ __forceinline__ void tile_diag_df(dfc *tile, int t, int L,
 template <typename T, int KMAX, bool S>
 __device__ __forceinline__ void smem_op(typename CT<T>::C *tile, int t, int L,
                                         const unsigned long long *rowoff, const TileOpDev &op,
-                                        const typename CT<T>::C *md, const void *tables) {
+                                        const typename CT<T>::C *md, const void *tables,
+                                        const Team &tm) {
   // diagonal tables are read from global memory (op.data: entry offset)
   const typename CT<T>::C *gt = reinterpret_cast<const typename CT<T>::C *>(tables) + op.data;
   if (op.kind == 2) {
     switch (op.k) {
-      case 1: tile_perm<T, 1, S>(tile, t, op); break;
-      case 2: tile_perm<T, 2, S>(tile, t, op); break;
-      case 3: if constexpr (KMAX >= 3) tile_perm<T, 3, S>(tile, t, op); break;
-      case 4: if constexpr (KMAX >= 4) tile_perm<T, 4, S>(tile, t, op); break;
-      case 5: if constexpr (KMAX >= 5) tile_perm<T, 5, S>(tile, t, op); break;
+      case 1: tile_perm<T, 1, S>(tile, t, op, tm); break;
+      case 2: tile_perm<T, 2, S>(tile, t, op, tm); break;
+      case 3: if constexpr (KMAX >= 3) tile_perm<T, 3, S>(tile, t, op, tm); break;
+      case 4: if constexpr (KMAX >= 4) tile_perm<T, 4, S>(tile, t, op, tm); break;
+      case 5: if constexpr (KMAX >= 5) tile_perm<T, 5, S>(tile, t, op, tm); break;
     }
     return;
   }
   if constexpr (kIsDf<T>) {
     if (op.kind == 0) {
       switch (op.k) {
-        case 1: tile_dense_df<1, S>(tile, t, op, md); break;
-        case 2: tile_dense_df<2, S>(tile, t, op, md); break;
-        case 3: if constexpr (KMAX >= 3) tile_dense_df<3, S>(tile, t, op, md); break;
-        case 4: if constexpr (KMAX >= 4) tile_dense_df<4, S>(tile, t, op, md); break;
-        case 5: if constexpr (KMAX >= 5) tile_dense_df<5, S>(tile, t, op, md); break;
+        case 1: tile_dense_df<1, S>(tile, t, tm, op, md); break;
+        case 2: tile_dense_df<2, S>(tile, t, tm, op, md); break;
+        case 3: if constexpr (KMAX >= 3) tile_dense_df<3, S>(tile, t, tm, op, md); break;
+        case 4: if constexpr (KMAX >= 4) tile_dense_df<4, S>(tile, t, tm, op, md); break;
+        case 5: if constexpr (KMAX >= 5) tile_dense_df<5, S>(tile, t, tm, op, md); break;
       }
     } else {
-      tile_diag_df<S>(tile, t, L, rowoff, op, gt);
+      tile_diag_df<S>(tile, t, L, rowoff, op, gt, tm);
     }
   } else {
     if (op.kind == 0) {
       switch (op.k) {
-        case 1: tile_dense<T, 1, S>(tile, t, op, md); break;
-        case 2: tile_dense<T, 2, S>(tile, t, op, md); break;
-        case 3: if constexpr (KMAX >= 3) tile_dense<T, 3, S>(tile, t, op, md); break;
-        case 4: if constexpr (KMAX >= 4) tile_dense<T, 4, S>(tile, t, op, md); break;
-        case 5: if constexpr (KMAX >= 5) tile_dense<T, 5, S>(tile, t, op, md); break;
+        case 1: tile_dense<T, 1, S>(tile, t, op, md, tm); break;
+        case 2: tile_dense<T, 2, S>(tile, t, op, md, tm); break;
+        case 3: if constexpr (KMAX >= 3) tile_dense<T, 3, S>(tile, t, op, md, tm); break;
+        case 4: if constexpr (KMAX >= 4) tile_dense<T, 4, S>(tile, t, op, md, tm); break;
+        case 5: if constexpr (KMAX >= 5) tile_dense<T, 5, S>(tile, t, op, md, tm); break;
       }
     } else {
-      tile_diag<T, S>(tile, t, L, rowoff, op, gt);
+      tile_diag<T, S>(tile, t, L, rowoff, op, gt, tm);
     }
   }
 }
 
 // KMAX: widest op of the pass; RB: register bits of the register stages
-// (0: every stage runs in shared memory).  Narrow instantiations keep the
-// register arrays of wide cases out of the kernel.
-// Threads of a tile CTA: 256, plus the MMA-issuing warp in tensor-core kernels.
+// (0: every stage runs in shared memory; -1: the pass has tensor-core ops).
+// Narrow instantiations keep the register arrays of wide cases out of the
+// kernel.  Threads of a tile CTA: 128 for the FMA engine, 256 with register
+// stages and for double-float tiles, 256 plus the MMA-issuing warp in
+// tensor-core kernels.
 template <typename T, int RB>
 constexpr int tile_threads() {
   return RB == 0 && !kIsDf<T> ? kTileThreadsSmem : (RB < 0 ? kTileThreads + 32 : kTileThreads);
+}
+
+// A tile's global base index (its element 0) and the offset of its row r of
+// 2^L contiguous amplitudes.
+__device__ __forceinline__ unsigned long long tile_base_index(const TileArgs &p,
+                                                              unsigned long long c) {
+  unsigned long long base = c << p.L;
+  for (int e = 0; e < p.nE; ++e) {
+    const int q = p.E[e];
+    const unsigned long long lo = base & ((1ull << q) - 1ull);
+    base = ((base >> q) << (q + 1)) | lo;
+  }
+  return base;
+}
+__device__ __forceinline__ unsigned long long tile_row_offset(const TileArgs &p,
+                                                              unsigned long long base, unsigned r) {
+  unsigned long long o = base;
+  for (int e = 0; e < p.nE; ++e)
+    if ((r >> e) & 1u) o |= 1ull << p.E[e];
+  return o;
 }
 
 template <typename T, int KMAX, int RB>
@@ -853,6 +896,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   __shared__ __align__(8) unsigned long long tc_mbar[2];
   __shared__ uint32_t tc_tmem_slot;
   __shared__ int tc_abort;
+  const Team tm{threadIdx.x, blockDim.x, (threadIdx.x >> 5) & 3u};
   TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1};
   if constexpr (RB < 0) {
     if ((threadIdx.x >> 5) == 0) {
@@ -909,18 +953,8 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   const unsigned rowmask = (1u << L) - 1u;
   for (unsigned long long c = blockIdx.x; c < p.ntiles; c += gridDim.x) {
     __syncthreads();  // previous tile's stores done before rowoff/tile reuse
-    unsigned long long base = c << L;
-    for (int e = 0; e < p.nE; ++e) {
-      int q = p.E[e];
-      unsigned long long lo = base & ((1ull << q) - 1ull);
-      base = ((base >> q) << (q + 1)) | lo;
-    }
-    for (unsigned r = threadIdx.x; r < nrows; r += blockDim.x) {
-      unsigned long long o = base;
-      for (int e = 0; e < p.nE; ++e)
-        if ((r >> e) & 1u) o |= 1ull << p.E[e];
-      rowoff[r] = o;
-    }
+    const unsigned long long base = tile_base_index(p, c);
+    for (unsigned r = threadIdx.x; r < nrows; r += blockDim.x) rowoff[r] = tile_row_offset(p, base, r);
     __syncthreads();
     for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
       unsigned el = ch * per16;
@@ -950,15 +984,16 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
       if constexpr (RB < 0) {
         if (op.kind == 3) {
           const unsigned char *bm = reinterpret_cast<const unsigned char *>(data + op.data);
-          if (op.k == 3) tile_tc<3>(reinterpret_cast<float2 *>(tile), t, op, bm, ctx, &tc_abort);
-          else if (op.k == 4) tile_tc<4>(reinterpret_cast<float2 *>(tile), t, op, bm, ctx, &tc_abort);
-          else tile_tc<5>(reinterpret_cast<float2 *>(tile), t, op, bm, ctx, &tc_abort);
+          float2 *ft = reinterpret_cast<float2 *>(tile);
+          if (op.k == 3) tile_tc<3>(ft, t, op, bm, ctx, &tc_abort, tm);
+          else if (op.k == 4) tile_tc<4>(ft, t, op, bm, ctx, &tc_abort, tm);
+          else tile_tc<5>(ft, t, op, bm, ctx, &tc_abort, tm);
           if (!ctx.ok) break;
           __syncthreads();
           continue;
         }
       }
-      smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data, p.tables);
+      smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data, p.tables, tm);
       __syncthreads();
     }
     if constexpr (RB < 0) {

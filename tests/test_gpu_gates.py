@@ -264,6 +264,37 @@ def test_tensor_core_tiles(gpu, oracle, fw, tile):
     s.free()
 
 
+def test_tensor_core_pass_diagonal_on_each_tile_bit(gpu, oracle):
+    """A 4-qubit block (a tensor-core op) and then an RZ that cannot join it
+    (diagonals join blocks of at most two qubits) leave a diagonal op in the
+    tensor-core pass.  Gates on qubits 5..12 only give the tile bits 5..12 to
+    those qubits, so the RZ walks through every tile bit of the pass.  The
+    diagonal op's threads each take a fixed stride of elements; with a
+    stride that is not a power of two (a 288-thread team) a phase read once
+    per thread would cover elements whose tile bit 8 differs."""
+    n = 18
+    rng = np.random.default_rng(12)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    init /= np.linalg.norm(init)
+    for q in range(5, 13):
+        others = [x for x in (6, 9, 12, 10) if x != q][:3]
+        gs = [(gates.haar_unitary(rng, 16), [q] + others), (gates.gate_matrix("RZ", 0.9), [q])]
+        p = Program()
+        p.add_gates(gs)
+        p.set_tensor_cores(True)
+        p.plan(n, "fp32", fused=True, fusion_width=2, tile_qubits=13)
+        (ps,) = p.describe()["passes"]
+        assert [op["kind"] for op in ps["ops"]] == ["tc", "diag"], ps["ops"]
+        assert ps["ops"][1]["tpos"] == [q] and ps["ops"][1]["req_tile"] == []
+        s = CudaPureState(n, "fp32")
+        s.set_state_elements(init)
+        p.run(s, fused=True)
+        want = _oracle(oracle, gs, n, init)
+        assert np.max(np.abs(s.state_elements() - want)) < 4e-6, q
+        s.free()
+        p.free()
+
+
 def test_tensor_core_fidelity_26q(gpu):
     """Fused FP32 with the tensor-core engine vs plain FP64 at 26 qubits."""
     n = 26
