@@ -588,10 +588,37 @@ __device__ __forceinline__ void bf16_split(float2 v, uint32_t &hi, uint32_t &lo)
   lo = *reinterpret_cast<const uint32_t *>(&l);
 }
 
+// Where the last op of a tensor-core pass puts its results: straight into
+// the state in HBM instead of back into the tile (the pass then skips its
+// store loop), and, once every chunk has been gathered, the tile buffer
+// takes the next tile's loads while the MMAs and the readout run.
+struct TcOut {
+  float2 *a;                      // the state
+  unsigned long long base;        // global index of this tile's element 0
+  const unsigned long long *dep;  // row r of a tile sits at base | dep[r]
+  int L;                          // row bits (2^L contiguous amplitudes)
+  bool next;                      // a next tile to load
+  unsigned long long next_base;
+};
+
+// The loads of a tile into the tile buffer: 16-byte asynchronous copies of
+// its rows, every copy of the team in flight at once.
+__device__ __forceinline__ void tile_load_async(float2 *tile, int t, const float2 *a,
+                                                unsigned long long base,
+                                                const unsigned long long *dep, int L,
+                                                const Team &tm) {
+  const unsigned nchunks = (1u << t) / 2, rowmask = (1u << L) - 1u;
+  for (unsigned ch = tm.id; ch < nchunks; ch += tm.n) {
+    const unsigned el = 2 * ch;
+    cp_async16(tile + el, a + (base | dep[el >> L]) + (el & rowmask));
+  }
+}
+
 template <int K>
 __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op,
                                         const unsigned char *bmat, TcCtx &ctx,
-                                        volatile int *abort_flag, const Team &tm) {
+                                        volatile int *abort_flag, const Team &tm,
+                                        const TcOut *out) {
   constexpr int D = 1 << K, NC = 2 * D, H = D / 2;
   constexpr uint32_t kSboB = 2 * 16 * D;   // Bt rows hold 2D bf16 (4D bytes); 8 rows per group
   constexpr uint32_t kPieceB = 8 * D * D;  // bytes of Bt hi (then Bt lo)
@@ -667,6 +694,10 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
       ctx.phase[0] ^= 1u;  // back to the phase of the commit that was not seen
       return;
     }
+    // every chunk gathered: a last op hands the tile buffer to the next tile
+    const bool load_next = out && out->next && base + kBufs >= nchunks;
+    if (load_next && !issuer)
+      tile_load_async(tile, t, out->a, out->next_base, out->dep, out->L, tm);
     if (issuer) {
       if (lane == 0) {
         for (unsigned c = 0; c < nb; ++c) {
@@ -687,6 +718,7 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
                 ctx.mbar[0])
             : "memory");
       }
+      if (load_next) tile_load_async(tile, t, out->a, out->next_base, out->dep, out->L, tm);
     } else {
       if (!tc_wait(ctx.mbar[0], ctx.phase[0])) {
         *abort_flag = 1;  // seen by every thread after the next barrier
@@ -697,10 +729,21 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
           tmem_ld<D>(ctx.tmem + c * kBufCols + lanes + half * D, r);
           asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
           const unsigned b = group_base(base + c);
+          if (out) {
+            // into HBM: the row deposit is linear over the disjoint bits of
+            // the group base and the block offset
+            const unsigned rowmask = (1u << out->L) - 1u;
+            float2 *g = out->a + (out->base | out->dep[b >> out->L]);
 #pragma unroll
-          for (int i = 0; i < H; ++i)
-            tile[b | off[i]] =
-                make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+            for (int i = 0; i < H; ++i)
+              g[out->dep[off[i] >> out->L] + ((b | off[i]) & rowmask)] =
+                  make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+          } else {
+#pragma unroll
+            for (int i = 0; i < H; ++i)
+              tile[b | off[i]] =
+                  make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+          }
         }
       }
     }
@@ -896,6 +939,7 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   __shared__ __align__(8) unsigned long long tc_mbar[2];
   __shared__ uint32_t tc_tmem_slot;
   __shared__ int tc_abort;
+  __shared__ unsigned long long tc_base;  // the tile's element 0 (a diagonal op's row offset 0)
   const Team tm{threadIdx.x, blockDim.x, (threadIdx.x >> 5) & 3u};
   TcCtx ctx{0u, {0u, 0u}, {0u, 0u}, 1};
   if constexpr (RB < 0) {
@@ -939,6 +983,9 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     for (int i = threadIdx.x; i < swords; i += blockDim.x) st[i] = gt[i];
   }
   if constexpr (RB < 0) {
+    // tensor-core passes keep the pass's row deposits (row r of a tile at
+    // its base | rowoff[r]) instead of per-tile row offsets
+    for (unsigned r = threadIdx.x; r < nrows; r += blockDim.x) rowoff[r] = tile_row_offset(p, 0ull, r);
     // the tensor core reads the operands in the pass data through the async proxy
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -951,62 +998,97 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
   constexpr int per16 = 16 / sizeof(C);  // amplitudes per 16-byte chunk
   const unsigned nchunks = (1u << t) / per16;
   const unsigned rowmask = (1u << L) - 1u;
-  for (unsigned long long c = blockIdx.x; c < p.ntiles; c += gridDim.x) {
-    __syncthreads();  // previous tile's stores done before rowoff/tile reuse
-    const unsigned long long base = tile_base_index(p, c);
-    for (unsigned r = threadIdx.x; r < nrows; r += blockDim.x) rowoff[r] = tile_row_offset(p, base, r);
-    __syncthreads();
-    for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
-      unsigned el = ch * per16;
-      const typename GT<T>::G *src = a + rowoff[el >> L] + (el & rowmask);
-      cp_async16(tile + sw<(RB > 0)>(el), src);
-    }
-    cp_async_wait_all();
-    if constexpr (kIsDf<T>) {
-      // this thread's own copies have landed: FP64 -> double-float in place
-      for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
-        dfc &d = tile[ch];
-        d = df_from_double2(*reinterpret_cast<const double2 *>(&d));
-      }
-    }
-    __syncthreads();
-    for (int s = 0; s < p.nstages; ++s) {
-      const TileStageDev &st = stages[s];
-      if constexpr (RB > 0) {
-        if (st.reg) {
-          reg_stage<RB>(reinterpret_cast<float2 *>(tile), t, st, ops,
-                        reinterpret_cast<const float2 *>(data));
-          __syncthreads();
-          continue;
-        }
-      }
-      const TileOpDev &op = ops[st.first];
-      if constexpr (RB < 0) {
+  if constexpr (RB < 0) {
+    // A pass whose last op is a tensor-core op writes its results from the
+    // readout straight into HBM and loads the next tile under that op's
+    // MMAs (TcOut); other passes store the tile afterwards.
+    const float2 *ga = reinterpret_cast<const float2 *>(a);
+    bool loaded = false;  // this tile's loads were issued by the previous tile's last op
+    for (unsigned long long c = blockIdx.x; c < p.ntiles; c += gridDim.x) {
+      __syncthreads();  // the previous tile is done with the buffer and tc_base
+      const unsigned long long base = tile_base_index(p, c);
+      if (threadIdx.x == 0) tc_base = base;
+      if (!loaded) tile_load_async(reinterpret_cast<float2 *>(tile), t, ga, base, rowoff, L, tm);
+      cp_async_wait_all();
+      __syncthreads();
+      const unsigned long long cn = c + gridDim.x;
+      const bool has_next = cn < p.ntiles;
+      bool direct = false;
+      for (int s = 0; s < p.nstages; ++s) {
+        const TileOpDev &op = ops[stages[s].first];
         if (op.kind == 3) {
           const unsigned char *bm = reinterpret_cast<const unsigned char *>(data + op.data);
           float2 *ft = reinterpret_cast<float2 *>(tile);
-          if (op.k == 3) tile_tc<3>(ft, t, op, bm, ctx, &tc_abort, tm);
-          else if (op.k == 4) tile_tc<4>(ft, t, op, bm, ctx, &tc_abort, tm);
-          else tile_tc<5>(ft, t, op, bm, ctx, &tc_abort, tm);
+          const bool last = s == p.nstages - 1;
+          const TcOut o{reinterpret_cast<float2 *>(a), base, rowoff, L, has_next,
+                        has_next && last ? tile_base_index(p, cn) : 0ull};
+          const TcOut *po = last ? &o : nullptr;
+          if (op.k == 3) tile_tc<3>(ft, t, op, bm, ctx, &tc_abort, tm, po);
+          else if (op.k == 4) tile_tc<4>(ft, t, op, bm, ctx, &tc_abort, tm, po);
+          else tile_tc<5>(ft, t, op, bm, ctx, &tc_abort, tm, po);
           if (!ctx.ok) break;
-          __syncthreads();
-          continue;
+          direct = last;
+        } else {
+          smem_op<T, KMAX, false>(tile, t, L, &tc_base, op, data + op.data, p.tables, tm);
+        }
+        __syncthreads();
+      }
+      if (!ctx.ok) break;  // uniform: set after a block-wide vote
+      loaded = direct && has_next;
+      if (!direct) {
+        const unsigned rowmask = (1u << L) - 1u;
+        for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
+          const unsigned el = ch * per16;
+          __stcs(reinterpret_cast<int4 *>(a + (base | rowoff[el >> L]) + (el & rowmask)),
+                 *reinterpret_cast<const int4 *>(tile + el));
         }
       }
-      smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data, p.tables, tm);
+    }
+    cp_async_wait_all();  // a tile loaded ahead lands before the CTA ends
+  } else {
+    for (unsigned long long c = blockIdx.x; c < p.ntiles; c += gridDim.x) {
+      __syncthreads();  // previous tile's stores done before rowoff/tile reuse
+      const unsigned long long base = tile_base_index(p, c);
+      for (unsigned r = threadIdx.x; r < nrows; r += blockDim.x)
+        rowoff[r] = tile_row_offset(p, base, r);
       __syncthreads();
-    }
-    if constexpr (RB < 0) {
-      if (!ctx.ok) break;  // uniform: set after a block-wide vote
-    }
-    for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
-      unsigned el = ch * per16;
-      int4 *dst = reinterpret_cast<int4 *>(a + rowoff[el >> L] + (el & rowmask));
+      for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
+        unsigned el = ch * per16;
+        const typename GT<T>::G *src = a + rowoff[el >> L] + (el & rowmask);
+        cp_async16(tile + sw<(RB > 0)>(el), src);
+      }
+      cp_async_wait_all();
       if constexpr (kIsDf<T>) {
-        const double2 v = df_to_double2(tile[el]);
-        __stcs(dst, *reinterpret_cast<const int4 *>(&v));
-      } else {
-        __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB > 0)>(el)));
+        // this thread's own copies have landed: FP64 -> double-float in place
+        for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
+          dfc &d = tile[ch];
+          d = df_from_double2(*reinterpret_cast<const double2 *>(&d));
+        }
+      }
+      __syncthreads();
+      for (int s = 0; s < p.nstages; ++s) {
+        const TileStageDev &st = stages[s];
+        if constexpr (RB > 0) {
+          if (st.reg) {
+            reg_stage<RB>(reinterpret_cast<float2 *>(tile), t, st, ops,
+                          reinterpret_cast<const float2 *>(data));
+            __syncthreads();
+            continue;
+          }
+        }
+        const TileOpDev &op = ops[st.first];
+        smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data, p.tables, tm);
+        __syncthreads();
+      }
+      for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
+        unsigned el = ch * per16;
+        int4 *dst = reinterpret_cast<int4 *>(a + rowoff[el >> L] + (el & rowmask));
+        if constexpr (kIsDf<T>) {
+          const double2 v = df_to_double2(tile[el]);
+          __stcs(dst, *reinterpret_cast<const int4 *>(&v));
+        } else {
+          __stcs(dst, *reinterpret_cast<const int4 *>(tile + sw<(RB > 0)>(el)));
+        }
       }
     }
   }
