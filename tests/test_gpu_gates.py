@@ -5,6 +5,7 @@ FP32 within 2e-6 absolute per amplitude on normalised states and fidelity
 >= 1 - 1e-6.
 """
 import itertools
+import os
 
 import numpy as np
 import pytest
@@ -291,6 +292,32 @@ def test_tensor_core_pass_diagonal_on_each_tile_bit(gpu, oracle):
         p.run(s, fused=True)
         want = _oracle(oracle, gs, n, init)
         assert np.max(np.abs(s.state_elements() - want)) < 4e-6, q
+        s.free()
+        p.free()
+
+
+def test_tensor_core_tiles_per_cta(gpu, oracle):
+    """A tensor-core pass's last op writes its readout into HBM and loads the
+    CTA's next tile under its MMAs.  Against the oracle with few and many
+    tiles per CTA: 16 qubits (8 tiles, one per CTA: no next tile), 22 qubits
+    (512 tiles over 304 CTAs: one or two each) and 26 qubits on a yielding
+    state (priority -1: CTAs of 16 tiles)."""
+    oracle.set_workers(os.cpu_count() or 1)
+    for n, prio, depth in ((16, 0, 6), (22, 0, 4), (26, -1, 2)):
+        gs = circuits.random_su_circuit(n, depth=depth, seed=n)
+        want = _oracle(oracle, gs, n)
+        p = Program()
+        p.add_gates(gs)
+        p.set_tensor_cores(True)
+        p.plan(n, "fp32", fused=True, fusion_width=5, tile_qubits=13)
+        assert any(op["kind"] == "tc" for ps in p.describe()["passes"] if ps["kind"] == "tile"
+                   for op in ps["ops"])
+        s = CudaPureState(n, "fp32")
+        s.set_priority(prio)
+        p.run(s, fused=True)
+        got = s.state_elements()
+        assert np.max(np.abs(got - want)) < 4e-6, n
+        assert abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real >= 1 - 1e-6, n
         s.free()
         p.free()
 
