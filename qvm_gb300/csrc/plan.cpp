@@ -21,6 +21,10 @@
 //     cannot join the pass blocks its qubits for the rest of the pass, which
 //     keeps the op order on every qubit.
 //  3. Diagonal runs are folded into phase tables over <= 10 qubits.
+//  4. In FP32 plans for the tensor cores, each pass's dense ops are merged
+//     into blocks of up to min(5, max(3, fw)) tile bits (an op may move past
+//     ops on disjoint qubits), and the 3- to 5-qubit blocks become tcgen05
+//     ops with their matrix split into bf16 hi and lo parts (merge_tile_ops).
 #include "plan.h"
 
 #include <algorithm>

@@ -18,7 +18,10 @@
 //    planner laid out), permutations, and dense blocks, one group of 2^k
 //    amplitudes per thread (two groups sharing 16-byte words for FP32 1-/2-
 //    qubit blocks);
-//  - tensor-core stages: merged 3-/4-qubit blocks as tcgen05 MMAs.
+//  - tensor-core stages: merged 3- to 5-qubit blocks as tcgen05 MMAs in
+//    bf16x3 (tile_tc).  When a pass ends with one, that op writes its
+//    results straight into HBM and the tile buffer takes the CTA's next tile
+//    while its MMAs run (the pass then has no store loop).
 // In kernels with register stages shared memory is XOR-swizzled (bits 1..3
 // of a tile index are XORed with bits 4..12 folded) so that the lanes of a
 // warp spread over the banks in both the row-contiguous copies and the
@@ -443,7 +446,7 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 
 // ---- tensor-core ops (FP32 state, tcgen05, BF16x3) ----------------------------------
 //
-// A dense block on k = 3 or 4 tile bits is a real GEMM per chunk of 128
+// A dense block on k = 3, 4 or 5 tile bits is a real GEMM per chunk of 128
 // groups: D[g][n] = sum_kk A[g][kk] Bt[n][kk], with A[g] the group's 2^k
 // amplitudes as (re, im) pairs and Bt the block's real form (n = 2r + re/im
 // of output r).  Both operands are split into bf16 hi + lo parts and the
@@ -462,14 +465,15 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 // and commits them to an mbarrier that the data warps wait on with a
 // bounded loop.
 //
-// Chunks go in batches (four for 4-qubit blocks, eight for 3-qubit ones),
-// each chunk with its own TMEM buffer (D | A): a batch is gathered, its MMAs
-// issued together under one commit, and read out after one wait -- two
-// barriers per batch.
+// Chunks go in batches (two for 5-qubit blocks, four for 4-qubit ones, eight
+// for 3-qubit ones), each chunk with its own TMEM buffer (D | A): a batch is
+// gathered, its MMAs issued together under one commit, and read out after
+// one wait -- two barriers per batch.
 constexpr int kTcCols = 256;  // TMEM columns per CTA
 // A chunk of a k-qubit block takes 4 * 2^k TMEM columns: D (2^(k+1) FP32
 // outputs) then A (2^k columns of hi, 2^k of lo, bf16 pairs); a batch is as
-// many chunks as the CTA's columns hold (4 for k = 4, 8 for k = 3).
+// many chunks as the CTA's columns hold (2 for k = 5, 4 for k = 4, 8 for
+// k = 3: on a 13-qubit tile, a whole op).
 constexpr int kTcWaitLimit = 1 << 20;  // tries of an MMA barrier wait before giving up
 
 struct TcCtx {
