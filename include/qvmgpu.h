@@ -93,6 +93,12 @@ int qvmg_device_reserve(uint64_t bytes);
  * fails with QVMG_E_NOMEM without reaching CUDA; 0 cancels.  Lets host-side
  * tests drive the out-of-memory paths without exhausting a shared GPU. */
 int qvmg_debug_fail_alloc(int nth);
+/* Test hook (no counterpart in the reference): while `on` is 1, the warp that
+ * issues a tensor-core tile op's MMAs issues none and commits nothing, so the
+ * op's bounded wait runs out (in about a second): the run returns
+ * QVMG_E_TIMEOUT, the kernel frees its tensor memory and the context stays
+ * usable.  Lets tests drive the timeout path with nothing in flight. */
+int qvmg_debug_tc_withhold(int on);
 /* HBM bytes a state of this size and precision holds (16*2^n or 8*2^n plus
  * its reduction scratch); 0 for invalid arguments. */
 uint64_t qvmg_state_bytes(int nqubits, int precision);

@@ -34,6 +34,7 @@ SIGNATURES = {
     "qvmg_last_error": (ctypes.c_char_p, []),
     "qvmg_abi_version": (_i, []),
     "qvmg_debug_fail_alloc": (_i, [_i]),
+    "qvmg_debug_tc_withhold": (_i, [_i]),
     "qvmg_device_info": (_i, [_ip, _u64p, _u64p]),
     "qvmg_state_bytes": (_u64, [_i, _i]),
     "qvmg_state_create": (_i, [_i, _i, _vpp]),

@@ -470,6 +470,9 @@ __device__ __forceinline__ void reg_stage(float2 *tile, int t, const TileStageDe
 // gathered, its MMAs issued together under one commit, and read out after
 // one wait -- two barriers per batch.
 constexpr int kTcCols = 256;  // TMEM columns per CTA
+// Test hook (qvmg_debug_tc_withhold): the MMA-issuing warp issues nothing,
+// so the data warps' bounded wait runs out.
+__device__ int g_tc_withhold = 0;
 // A chunk of a k-qubit block takes 4 * 2^k TMEM columns: D (2^(k+1) FP32
 // outputs) then A (2^k columns of hi, 2^k of lo, bf16 pairs); a batch is as
 // many chunks as the CTA's columns hold (2 for k = 5, 4 for k = 4, 8 for
@@ -703,7 +706,7 @@ __device__ __forceinline__ void tile_tc(float2 *tile, int t, const TileOpDev &op
     if (load_next && !issuer)
       tile_load_async(tile, t, out->a, out->next_base, out->dep, out->L, tm);
     if (issuer) {
-      if (lane == 0) {
+      if (lane == 0 && !g_tc_withhold) {
         for (unsigned c = 0; c < nb; ++c) {
           const uint32_t buf = ctx.tmem + c * kBufCols;
           const uint32_t a = buf + kACol;
@@ -1201,3 +1204,9 @@ int launch_tile(qvmg_state s, const TileArgs &args) {
 }
 
 }  // namespace qvmg
+
+extern "C" int qvmg_debug_tc_withhold(int on) {
+  const int v = on ? 1 : 0;
+  QVMG_CUDA(cudaMemcpyToSymbol(qvmg::g_tc_withhold, &v, sizeof(int)));
+  return QVMG_OK;
+}

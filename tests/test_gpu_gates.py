@@ -322,6 +322,41 @@ def test_tensor_core_tiles_per_cta(gpu, oracle):
         p.free()
 
 
+def test_tensor_core_wait_gives_up_and_context_recovers(gpu, oracle):
+    """The wait of a tensor-core op for its MMAs is bounded.  With the MMA
+    warp told to issue nothing (a test hook: nothing is in flight), the wait
+    runs out, the run reports QVMG_E_TIMEOUT through the status word, the
+    kernel frees its tensor memory, and the same program then runs correctly
+    on the same context."""
+    from qvm_gb300 import QVMGError
+    from qvm_gb300 import _lib as L
+    n = 16
+    rng = np.random.default_rng(31)
+    gs = [(gates.haar_unitary(rng, 16), [6, 9, 12, 10])]
+    p = Program()
+    p.add_gates(gs)
+    p.set_tensor_cores(True)
+    p.plan(n, "fp32", fused=True, fusion_width=2, tile_qubits=13)
+    (ps,) = p.describe()["passes"]
+    assert [op["kind"] for op in ps["ops"]] == ["tc"]
+    init = circuits.random_state(n, seed=32)
+    s = CudaPureState(n, "fp32")
+    s.set_state_elements(init)
+    L.call("qvmg_debug_tc_withhold", 1)
+    try:
+        with pytest.raises(QVMGError, match="timed out") as err:
+            p.run(s, fused=True)
+        assert err.value.code == 6  # QVMG_E_TIMEOUT
+    finally:
+        L.call("qvmg_debug_tc_withhold", 0)
+    s.set_state_elements(init)
+    p.run(s, fused=True)
+    want = _oracle(oracle, gs, n, init)
+    assert np.max(np.abs(s.state_elements() - want)) < 4e-6
+    s.free()
+    p.free()
+
+
 def test_tensor_core_fidelity_26q(gpu):
     """Fused FP32 with the tensor-core engine vs plain FP64 at 26 qubits."""
     n = 26
