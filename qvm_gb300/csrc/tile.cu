@@ -1012,7 +1012,9 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     const float2 *ga = reinterpret_cast<const float2 *>(a);
     bool loaded = false;  // this tile's loads were issued by the previous tile's last op
     for (unsigned long long c = blockIdx.x; c < p.ntiles; c += gridDim.x) {
-      __syncthreads();  // the previous tile is done with the buffer and tc_base
+      // the previous tile's store loop is done with the buffer (a last op
+      // that loaded this tile ended with its own barrier)
+      if (!loaded) __syncthreads();
       const unsigned long long base = tile_base_index(p, c);
       if (threadIdx.x == 0) tc_base = base;
       if (!loaded) tile_load_async(reinterpret_cast<float2 *>(tile), t, ga, base, rowoff, L, tm);
@@ -1034,11 +1036,11 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
           else if (op.k == 4) tile_tc<4>(ft, t, op, bm, ctx, &tc_abort, tm, po);
           else tile_tc<5>(ft, t, op, bm, ctx, &tc_abort, tm, po);
           if (!ctx.ok) break;
-          direct = last;
+          direct = last;  // tile_tc ends with a barrier after its readout
         } else {
           smem_op<T, KMAX, false>(tile, t, L, &tc_base, op, data + op.data, p.tables, tm);
+          __syncthreads();
         }
-        __syncthreads();
       }
       if (!ctx.ok) break;  // uniform: set after a block-wide vote
       loaded = direct && has_next;
