@@ -95,7 +95,7 @@ def test_fused_plan_equals_circuit(oracle, prec, fw, tile):
             assert st["source_ops"] == len(gs)
 
 
-@pytest.mark.parametrize("fw,tile", [(2, 0), (4, 0), (2, 11), (4, 12), (1, 13), (5, 13)])
+@pytest.mark.parametrize("fw,tile", [(2, 0), (4, 0), (2, 11), (4, 12), (1, 13), (5, 13), (5, 14)])
 def test_tensor_core_plan_equals_circuit(oracle, fw, tile):
     """FP32 tensor-core planning: the pass-local merge into blocks of up to
     the fusion width's tile bits (3..5) and the split bf16 operand, executed on the oracle, equal the

@@ -244,11 +244,12 @@ def test_register_stages(gpu, oracle, tile):
     s.free()
 
 
-@pytest.mark.parametrize("fw,tile", [(2, 13), (4, 13), (4, 12), (3, 11), (5, 13)])
+@pytest.mark.parametrize("fw,tile", [(2, 13), (4, 13), (4, 12), (3, 11), (5, 13), (5, 14)])
 def test_tensor_core_tiles(gpu, oracle, fw, tile):
     """FP32 tiles whose merged 3- to 5-qubit blocks run as tcgen05 bf16x3
     MMAs (hi/lo split operands), mixed with 2-qubit FMA blocks, permutations
-    and diagonal tables.  The MMA accumulator rounds toward zero, which shrinks
+    and diagonal tables (14-qubit tiles: a 5-qubit op takes two TMEM batches,
+    the first read out into HBM before the second is gathered).  The MMA accumulator rounds toward zero, which shrinks
     the norm by ~1e-7 per block; the comparison is per amplitude (4e-6) and
     as a normalised overlap (1 - 1e-6)."""
     n = 18
