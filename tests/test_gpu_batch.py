@@ -179,3 +179,34 @@ def test_qaoa_batch_wide_instances_match_oracle(gpu, oracle):
             near = np.array([np.min(np.abs(cdf - d * tot)) < 1e-9 for d in draws[i]])
             assert ((shots[i] == wsh) | near).all(), (p, n)
         b.free()
+
+
+@pytest.mark.parametrize("p", [7, 8])
+def test_qaoa_batch_deep_circuits_match_oracle(gpu, oracle, p):
+    """Depths 7 and 8: the p + 1 tile passes of an instance in HBM alternate
+    between contiguous tiles and high-qubit rows p + 1 times, each finishing
+    one layer's RX and starting the next; an odd depth ends on a row pass (the
+    CDF and <H_C> read back from HBM), an even one on a contiguous pass (both
+    summed from the tiles).  Beside them, instances that stay in shared
+    memory.  Against the oracle: amplitudes, <H_C> and 256 shots each."""
+    oracle.set_workers(os.cpu_count() or 1)
+    rng = np.random.default_rng(40 + p)
+    graphs = [(n, circuits.random_3_regular_graph(n, rng)) for n in (10, 16, 20, 14)]
+    gam = rng.uniform(0, np.pi, (len(graphs), p))
+    bet = rng.uniform(0, np.pi / 2, (len(graphs), p))
+    b = QaoaBatch(graphs, gam, bet)
+    draws = np.random.default_rng(50 + p).random((len(graphs), 256))
+    ex, shots = b.run(draws)
+    for i, (n, edges) in enumerate(graphs):
+        want = oracle_qaoa(oracle, n, edges, gam[i], bet[i])
+        got = b.state(i)
+        assert np.max(np.abs(got - want)) < 4e-6, (p, n)
+        wex = float(np.sum(np.abs(want) ** 2 * circuits.maxcut_values(n, edges)))
+        assert abs(ex[i] - wex) < 1e-5 * max(1.0, wex), (p, n, ex[i], wex)
+        ref = got.astype(np.complex64).astype(np.complex128)
+        tot = np.sum(np.abs(ref) ** 2)
+        wsh = oracle.sample_multiple(ref, draws[i] * tot)
+        cdf = np.cumsum(np.abs(ref) ** 2)
+        near = np.array([np.min(np.abs(cdf - d * tot)) < 1e-9 for d in draws[i]])
+        assert ((shots[i] == wsh) | near).all(), (p, n)
+    b.free()
