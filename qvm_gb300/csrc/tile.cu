@@ -79,9 +79,22 @@ struct Team {
 // amplitude, with every output summed in the same order (bit-identical):
 // 296 against 303 ms for the 30-qubit depth-20 circuit, 638 against 699 ms
 // unfused.
+// Where a pass's last op may write its output: straight into the state in
+// HBM (element p of the tile at rowoff[p >> L] + (p & (2^L - 1))) instead of
+// the tile, so that the pass needs no store loop.
+struct TileOut {
+  float2 *a;
+  const unsigned long long *rowoff;
+  int L;
+  __device__ __forceinline__ float4 *at(unsigned p) const {
+    return reinterpret_cast<float4 *>(a + rowoff[p >> L] + (p & ((1u << L) - 1u)));
+  }
+};
+
 template <int K, int J0>
 __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 *m,
-                                              const unsigned *off, const int *sp, const Team &tm) {
+                                              const unsigned *off, const int *sp, const Team &tm,
+                                              const TileOut *out) {
   constexpr int D = 1 << K;
   float4 *t4 = reinterpret_cast<float4 *>(tile);
   if constexpr (J0 >= 0) {
@@ -112,7 +125,9 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
       for (int r = 0; r < D; ++r)
         if (!((r >> J0) & 1)) {
           const float2 a = o[r], e = o[r | (1 << J0)];
-          t4[(b | off[r]) >> 1] = make_float4(a.x, a.y, e.x, e.y);
+          const float4 w = make_float4(a.x, a.y, e.x, e.y);
+          if (out) __stcs(out->at(b | off[r]), w);
+          else t4[(b | off[r]) >> 1] = w;
         }
     }
   } else {
@@ -137,7 +152,9 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
           cmac(a, m[r * D + c], va[c]);
           cmac(e, m[r * D + c], vb[c]);
         }
-        t4[(b | off[r]) >> 1] = make_float4(a.x, a.y, e.x, e.y);
+        const float4 w = make_float4(a.x, a.y, e.x, e.y);
+        if (out) __stcs(out->at(b | off[r]), w);
+        else t4[(b | off[r]) >> 1] = w;
       }
     }
   }
@@ -145,7 +162,8 @@ __device__ __forceinline__ void tile_dense_v4(float2 *tile, int t, const float2 
 
 template <typename T, int K, bool S>
 __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const TileOpDev &op,
-                                           const typename CT<T>::C *mat, const Team &tm) {
+                                           const typename CT<T>::C *mat, const Team &tm,
+                                           const TileOut *out = nullptr) {
   using C = typename CT<T>::C;
   constexpr int D = 1 << K;
   int sp[K];
@@ -181,9 +199,9 @@ __device__ __forceinline__ void tile_dense(typename CT<T>::C *tile, int t, const
     for (int i = 0; i < D * D; ++i) mreg[i] = mat[i];
   }
   if constexpr (std::is_same<T, float>::value && !S && K <= 2) {
-    if (op.pos[0] == 0) tile_dense_v4<K, 0>(tile, t, mreg, off, sp, tm);
-    else if (K == 2 && op.pos[K - 1] == 0) tile_dense_v4<K, K - 1>(tile, t, mreg, off, sp, tm);
-    else tile_dense_v4<K, -1>(tile, t, mreg, off, sp, tm);
+    if (op.pos[0] == 0) tile_dense_v4<K, 0>(tile, t, mreg, off, sp, tm, out);
+    else if (K == 2 && op.pos[K - 1] == 0) tile_dense_v4<K, K - 1>(tile, t, mreg, off, sp, tm, out);
+    else tile_dense_v4<K, -1>(tile, t, mreg, off, sp, tm, out);
     return;
   }
   const unsigned ngroups = 1u << (t - K);
@@ -1055,6 +1073,16 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
     }
     cp_async_wait_all();  // a tile loaded ahead lands before the CTA ends
   } else {
+    // An FP32 FMA pass whose last op is a 1-/2-qubit dense block writes that
+    // op's output pairs straight into HBM (TileOut): no store loop.
+    bool direct = false;
+    if constexpr (std::is_same<T, float>::value && RB == 0) {
+      __syncthreads();  // the op and stage descriptors are in shared memory
+      if (p.nstages > 0) {
+        const TileOpDev &lop = ops[stages[p.nstages - 1].first];
+        direct = lop.kind == 0 && lop.k <= 2;
+      }
+    }
     for (unsigned long long c = blockIdx.x; c < p.ntiles; c += gridDim.x) {
       __syncthreads();  // previous tile's stores done before rowoff/tile reuse
       const unsigned long long base = tile_base_index(p, c);
@@ -1086,9 +1114,18 @@ __global__ void __launch_bounds__(tile_threads<T, RB>(), (RB == 5 || RB < 0) ? 2
           }
         }
         const TileOpDev &op = ops[st.first];
+        if constexpr (std::is_same<T, float>::value && RB == 0) {
+          if (direct && s == p.nstages - 1) {
+            const TileOut o{reinterpret_cast<float2 *>(a), rowoff, L};
+            if (op.k == 1) tile_dense<float, 1, false>(tile, t, op, data + op.data, tm, &o);
+            else tile_dense<float, 2, false>(tile, t, op, data + op.data, tm, &o);
+            continue;  // the next tile's first barrier orders the buffer's reuse
+          }
+        }
         smem_op<T, KMAX, (RB > 0)>(tile, t, L, rowoff, op, data + op.data, p.tables, tm);
         __syncthreads();
       }
+      if (direct) continue;
       for (unsigned ch = threadIdx.x; ch < nchunks; ch += blockDim.x) {
         unsigned el = ch * per16;
         int4 *dst = reinterpret_cast<int4 *>(a + rowoff[el >> L] + (el & rowmask));
