@@ -105,7 +105,7 @@ def whole_job_rate(units_per_rank_step: int, steps: int, world: int, max_ms: flo
 # the ncu captures summarised under profiles/ (k_tile_fp32_random26_fw2_t13,
 # k_tile_tc_bf16x3_random26_fw5_t13).  Traffic per launch grows with the
 # amplitudes processed, so a launch at n qubits moves 2^(n-26) times as much.
-TILE_TRAFFIC_26Q = {"fma": 536.926208e6 + 475.259648e6, "tc": 536.993792e6 + 474.862848e6}
+TILE_TRAFFIC_26Q = {"fma": 536.987648e6 + 475.479808e6, "tc": 536.993792e6 + 474.862848e6}
 
 
 def traffic_per_launch(n, engine):
